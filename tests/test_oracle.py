@@ -1,0 +1,206 @@
+"""Pin the CPU oracle against the reference's own known-answer vectors (CPU only).
+
+Every vector comes from ``tests/golden/reference_vectors.json``, extracted from
+the reference's test files by ``tests/golden/make_golden.py``.
+"""
+import json
+import os
+import random
+
+import numpy as np
+import pytest
+
+from oracle import refpath, ring
+from oracle.yashe import Sampler, Yashe, YasheParams, round_div
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.json")))
+P = int(GOLD["goldilocks"]["P"])
+
+
+def test_primes_bucket_regenerates():
+    """PRIMES_BUCKET (src/polynomial.cpp:22) = the 100 largest primes below 2^29."""
+    vals = GOLD["primes_bucket"]["values"]
+    assert ring.primes_below_descending(2**29, len(vals)) == vals
+    assert refpath.bucket(len(vals)) == vals
+
+
+def test_mul_golden_vector_plain_product():
+    """src/test_mul.cu second test: a*b over Z for explicit 8-coefficient inputs."""
+    t = GOLD["test_mul_2"]
+    a = [int(x) for x in t["a"]]
+    b = [int(x) for x in t["b"]]
+    exp = [int(x) for x in t["expected_plain_product"]]
+    assert ring.plain_mul(a, b) == exp
+    assert ring.plain_mul_schoolbook(a, b) == exp
+    rp = refpath.RefPath(int(t["q"]), t["degree"])
+    assert rp.mul_plain(a, b) == exp
+
+
+def test_simple_multiply_by_polynomial():
+    """src/test.cu:421-470: a_i = i, b_i = 1 at degree 8, compared over Z_q."""
+    ps = GOLD["poly_suite"]
+    q, n = int(ps["q"]), ps["degree"]
+    a = list(range(n))
+    b = [1] * n
+    exp = [sum(range(min(k, n - 1) + 1)) - sum(range(max(0, k - n + 1))) for k in range(2 * n - 1)]
+    assert ring.plain_mul(a, b) == exp
+    rp = refpath.RefPath(q, n)
+    assert rp.mul_plain(a, b) == exp
+
+
+def test_smul_goldilocks():
+    """smulTest (src/test.cu:330-346): s_mul(a,b) == (a*b) mod P, both branches."""
+    rng = random.Random(36251)
+    for _ in range(2000):
+        a, b = rng.getrandbits(64), rng.getrandbits(64)
+        assert refpath.s_mul(a, b) == a * b % P
+        assert refpath.s_mul_device_formula(a, b) == a * b % P
+    for _ in range(2000):
+        a, b = rng.getrandbits(31), rng.getrandbits(31)
+        assert refpath.s_mul_device_formula(a, b) == a * b % P
+
+
+@pytest.mark.parametrize("n", [2, 8, 16, 8192])
+def test_wn_twiddles(n):
+    """wNTest (src/test.cu:305-329): w = 7^((P-1)/n) and W[j]*WInv[j] == 1 mod P."""
+    root = GOLD["goldilocks"]["root"]
+    assert refpath.omega(n) == pow(root, (P - 1) // n, P)
+    W, WI = refpath.twiddles(n)
+    assert all(x * y % P == 1 for x, y in zip(W, WI))
+
+
+def test_bnt_crt_roundtrip():
+    """src/test_bnt.cu:128-190: CRT then ICRT of 5342748479728798479824982."""
+    tb = GOLD["test_bnt_crt"]
+    X, q = int(tb["x"]), int(tb["q"])
+    rp = refpath.RefPath(q, tb["degree"])
+    primes = rp.primes()
+    words = ring.to_limbs([X], 2).reshape(-1).tolist()
+    res = [refpath.mod1_low(words, p) for p in primes]
+    assert res == [X % p for p in primes]
+    M = 1
+    for p in primes:
+        M *= p
+    back = sum((r * pow(M // p, -1, p) % p) * (M // p) for r, p in zip(res, primes)) % M
+    assert back == X
+
+
+def test_gen_crt_primes_rule():
+    """gen_crt_primes (src/polynomial.h:914): primes until M >= 2*degree*q^2."""
+    bucket = GOLD["primes_bucket"]["values"]
+    for q, deg in [(int(GOLD["poly_suite"]["q"]), 8), (2**127 - 1, 4096)]:
+        rp = refpath.RefPath(q, deg)
+        pr = rp.primes()
+        assert pr == bucket[: len(pr)]
+        M = 1
+        for p in pr:
+            M *= p
+        assert M >= 2 * deg * q * q
+        assert M // pr[-1] < 2 * deg * q * q
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 8, 33, 64])
+def test_kronecker_matches_schoolbook(n):
+    rng = random.Random(n)
+    for q in [97, 2**61 - 1, 2**127 - 1, 2**380 + 1]:
+        a = [rng.randrange(q) for _ in range(n)]
+        b = [rng.randrange(q) for _ in range(n)]
+        assert ring.plain_mul(a, b) == ring.plain_mul_schoolbook(a, b)
+        ac = [ring.centered(x, q) for x in a]
+        bc = [ring.centered(x, q) for x in b]
+        assert ring.plain_mul(ac, bc) == ring.plain_mul_schoolbook(ac, bc)
+
+
+@pytest.mark.parametrize("n", [4, 64, 1024])
+def test_ntt_mod_q_matches_kronecker(n):
+    q = ring.largest_prime_below(2**127, 2**16)
+    rng = random.Random(n)
+    a = [rng.randrange(q) for _ in range(n)]
+    b = [rng.randrange(q) for _ in range(n)]
+    assert ring.NttModQ(n, q).mul(a, b) == ring.polymul_mod(a, b, q)
+
+
+def test_poly_inverse_both_methods():
+    rng = random.Random(5)
+    q = int(GOLD["yashe_suite"]["q"])  # = 5 mod 8: extended Euclid
+    for n in [4, 8, 16]:
+        f = [rng.randrange(q) for _ in range(n)]
+        fi = ring.poly_inverse_mod(f, q)
+        assert ring.polymul_mod(f, fi, q) == [1] + [0] * (n - 1)
+    q2 = ring.largest_prime_below(2**62, 2**16)
+    f = [rng.randrange(q2) for _ in range(256)]
+    fi = ring.poly_inverse_mod(f, q2)
+    assert ring.polymul_mod(f, fi, q2) == [1] + [0] * 255
+
+
+def test_refpath_matches_oracle_where_reference_is_exact():
+    """The reference multiply is exact while n*c < P (integer NTTScale,
+    src/cuda_functions.cu:397-402). Small-magnitude inputs stay in that regime at
+    any N; full-size inputs at N = 8 (the reference's own test size) almost always do."""
+    q = int(GOLD["poly_suite"]["q"])
+    rng = random.Random(7)
+    rp = refpath.RefPath(q, 8)
+    ok = 0
+    for _ in range(40):
+        a = [rng.randrange(q) for _ in range(8)]
+        b = [rng.randrange(q) for _ in range(8)]
+        c = ring.from_limbs(rp.polymul(ring.to_limbs(a, 2)[None], ring.to_limbs(b, 2)[None]))
+        ok += c == ring.polymul_mod(a, b, q)
+    assert ok >= 36
+    n = 256
+    rp = refpath.RefPath(2**127 - 1, n)
+    a = [rng.randrange(2**12) for _ in range(n)]
+    b = [rng.randrange(2**12) for _ in range(n)]
+    c = ring.from_limbs(rp.polymul(ring.to_limbs(a, 2)[None], ring.to_limbs(b, 2)[None], nthreads=4))
+    assert c == ring.polymul_mod(a, b, 2**127 - 1)
+
+
+def test_refpath_defect_at_full_size():
+    """Documents the reference defect: at N = 64 with full-size residues the
+    integer division in NTTScale breaks the product."""
+    q = 2**127 - 1
+    rng = random.Random(9)
+    rp = refpath.RefPath(q, 64)
+    a = [rng.randrange(q) for _ in range(64)]
+    b = [rng.randrange(q) for _ in range(64)]
+    c = ring.from_limbs(rp.polymul(ring.to_limbs(a, 2)[None], ring.to_limbs(b, 2)[None]))
+    assert c != ring.polymul_mod(a, b, q)
+
+
+def test_round_div_matches_reference_rounding():
+    rng = random.Random(3)
+    q = 2**127 - 1
+    for _ in range(1000):
+        x = rng.randrange(-(2**260), 2**260)
+        quot, diff = divmod(x, q)
+        exp = quot + 1 if 2 * diff > q else quot
+        assert round_div(x, q) == exp
+
+
+@pytest.mark.parametrize("n,qbits,t", [(4, None, 35951), (16, 127, 1024), (256, 190, 65537)])
+def test_yashe_oracle_roundtrip(n, qbits, t):
+    if qbits is None:
+        q = int(GOLD["yashe_suite"]["q"])  # YasheSuite modulus, t = 35951, degree 4
+    else:
+        q = ring.largest_prime_below(2**qbits, 2**16)
+    Y = Yashe(YasheParams(n=n, q=q, t=t, w_bits=32))
+    K = Y.keygen(1234)
+    smp = Sampler(99)
+    m1, m2 = smp.uniform(n, t), smp.uniform(n, t)
+    c1, c2 = Y.encrypt(K, m1, 1), Y.encrypt(K, m2, 2)
+    assert Y.decrypt(K, c1) == m1
+    assert Y.decrypt(K, Y.add(c1, c2)) == [(x + y) % t for x, y in zip(m1, m2)]
+    expect = ring.polymul_mod(m1, m2, t)
+    ct = Y.mul_tensor(c1, c2)
+    assert Y.decrypt(K, ct, aftermul=True) == expect
+    cr = Y.keyswitch(K, ct)
+    assert Y.decrypt(K, cr) == expect
+    assert Y.noise(K, cr, expect) < Y.p.delta // 2
+
+
+def test_limbs_roundtrip():
+    rng = random.Random(1)
+    vals = [rng.getrandbits(190) for _ in range(17)]
+    arr = ring.to_limbs(vals, 3)
+    assert arr.dtype == np.uint64 and arr.shape == (17, 3)
+    assert ring.from_limbs(arr) == vals
