@@ -1,0 +1,263 @@
+"""Python mirror of the reference's host objects over the C ABI.
+
+``Ring``  ~ the reference's ``Polynomial`` arithmetic for one (N, q):
+            ``polymul`` = ``Polynomial c = a*b; c.reduce();`` (src/polynomial.cpp:52-60,
+            src/cuda_functions.cu:1040-1077), ``polyadd``/``polysub`` =
+            ``operator+``/``operator-`` followed by ``% q``, ``scalar_mul`` =
+            ``operator*(ZZ)`` (src/polynomial.h:533-573).
+``Yashe`` ~ ``Yashe`` + ``Ciphertext`` (src/yashe.h, src/ciphertext.h):
+            ``keygen``, ``encrypt``, ``decrypt``, ``mul`` (``Ciphertext::operator*``,
+            optionally followed by ``convert``), ``keyswitch`` (``convert``), ``add``.
+
+Polynomials are [batch][N][L] little-endian uint64 limbs. On the device they are
+torch int64 tensors holding the same bits; on the host numpy uint64 arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import (CY_OK, PolymulJob, RingInfo, YasheInfo, YasheParams, _ptr, _stream_handle, check, lib,
+               limbs_of)
+
+
+def nlimbs(q: int) -> int:
+    return max(1, ((q - 1).bit_length() + 63) // 64)
+
+
+def to_limb_array(values, L: int) -> np.ndarray:
+    """ints (nested lists ok) -> uint64 array with a trailing limb axis."""
+    arr = np.asarray(values, dtype=object)
+    flat = arr.reshape(-1)
+    raw = b"".join(int(v).to_bytes(8 * L, "little") for v in flat)
+    return np.frombuffer(raw, dtype="<u8").reshape(arr.shape + (L,)).copy()
+
+
+def from_limb_array(arr: np.ndarray):
+    a = np.ascontiguousarray(arr, dtype="<u8")
+    L = a.shape[-1]
+    flat = a.reshape(-1, L)
+    raw = flat.tobytes()
+    vals = [int.from_bytes(raw[i * 8 * L:(i + 1) * 8 * L], "little") for i in range(flat.shape[0])]
+    return np.array(vals, dtype=object).reshape(a.shape[:-1])
+
+
+def to_device(arr: np.ndarray, device="cuda"):
+    import torch
+    a = np.ascontiguousarray(arr, dtype=np.uint64)
+    return torch.from_numpy(a.view(np.int64)).to(device)
+
+
+def to_host(t) -> np.ndarray:
+    return t.detach().cpu().numpy().view(np.uint64)
+
+
+class Workspace:
+    """Scratch for calls issued on different streams at the same time."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().cy_workspace_create(ctypes.byref(h)), "cy_workspace_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().cy_workspace_destroy(self.h)
+            self.h = None
+
+
+class Ring:
+    """Z_q[x]/(x^N+1) on the GPU (handle to a ``cy_ring``)."""
+
+    def __init__(self, n: int, q: int, handle: Optional[ctypes.c_void_p] = None, owner=None):
+        self.n, self.q, self.L = n, q, nlimbs(q)
+        self._owner = owner
+        if handle is None:
+            h = ctypes.c_void_p()
+            check(lib().cy_ring_create(n, limbs_of(q, self.L), self.L, ctypes.byref(h)), "cy_ring_create")
+            self.h, self._own = h, True
+        else:
+            self.h, self._own = handle, False
+        info = RingInfo()
+        check(lib().cy_ring_get_info(self.h, ctypes.byref(info)), "cy_ring_get_info")
+        self.info = info
+        self.k = info.crt_primes
+        self.primes = [info.primes[i] for i in range(info.crt_primes)]
+
+    def __del__(self):
+        if getattr(self, "_own", False) and self.h.value:
+            lib().cy_ring_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    # -- buffers ----------------------------------------------------------
+    def empty(self, batch: int, device="cuda"):
+        import torch
+        return torch.empty((batch, self.n, self.L), dtype=torch.int64, device=device)
+
+    def upload(self, polys) -> "torch.Tensor":  # noqa: F821
+        """list of polynomials (lists of ints in [0, q)) or a limb array -> device tensor."""
+        arr = polys if isinstance(polys, np.ndarray) and polys.dtype == np.uint64 else to_limb_array(polys, self.L)
+        if arr.ndim == 2:
+            arr = arr[None]
+        return to_device(arr)
+
+    def download(self, t):
+        return from_limb_array(to_host(t))
+
+    # -- ops ----------------------------------------------------------------
+    def polymul(self, a, b, out=None, stream=None, workspace: Optional[Workspace] = None):
+        batch = a.shape[0]
+        out = self.empty(batch) if out is None else out
+        st = _stream_handle(stream)
+        if workspace is None:
+            check(lib().cy_polymul(self.h, _ptr(a), _ptr(b), _ptr(out), batch, st), "cy_polymul")
+        else:
+            check(lib().cy_polymul_ws(self.h, workspace.h, _ptr(a), _ptr(b), _ptr(out), batch, st), "cy_polymul_ws")
+        return out
+
+    def polymul_host(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        out = np.empty_like(a)
+        check(lib().cy_polymul_host(self.h, a.ctypes.data, b.ctypes.data, out.ctypes.data, a.shape[0]),
+              "cy_polymul_host")
+        return out
+
+    def polyadd(self, a, b, out=None, stream=None):
+        out = self.empty(a.shape[0]) if out is None else out
+        check(lib().cy_polyadd(self.h, _ptr(a), _ptr(b), _ptr(out), a.shape[0], _stream_handle(stream)),
+              "cy_polyadd")
+        return out
+
+    def polysub(self, a, b, out=None, stream=None):
+        out = self.empty(a.shape[0]) if out is None else out
+        check(lib().cy_polysub(self.h, _ptr(a), _ptr(b), _ptr(out), a.shape[0], _stream_handle(stream)),
+              "cy_polysub")
+        return out
+
+    def scalar_mul(self, a, s: int, out=None, stream=None):
+        out = self.empty(a.shape[0]) if out is None else out
+        check(lib().cy_poly_scalar_mul(self.h, _ptr(a), limbs_of(s, self.L), _ptr(out), a.shape[0],
+                                       _stream_handle(stream)), "cy_poly_scalar_mul")
+        return out
+
+    def residues_empty(self, batch: int):
+        import torch
+        return torch.empty((batch, self.k, self.n), dtype=torch.int32, device="cuda")
+
+    def crt(self, x, out=None, stream=None):
+        out = self.residues_empty(x.shape[0]) if out is None else out
+        check(lib().cy_crt(self.h, _ptr(x), _ptr(out), x.shape[0], _stream_handle(stream)), "cy_crt")
+        return out
+
+    def icrt(self, res, out=None, stream=None):
+        out = self.empty(res.shape[0]) if out is None else out
+        check(lib().cy_icrt(self.h, _ptr(res), _ptr(out), res.shape[0], _stream_handle(stream)), "cy_icrt")
+        return out
+
+    def ntt(self, res, inverse: bool = False, stream=None):
+        check(lib().cy_ntt(self.h, _ptr(res), res.shape[0], 1 if inverse else 0, _stream_handle(stream)), "cy_ntt")
+        return res
+
+
+def polymul_batched(jobs: Sequence[tuple], stream=None) -> None:
+    """jobs: (ring, a, b, c) with device tensors; one submission for mixed rings."""
+    arr = (PolymulJob * len(jobs))()
+    for i, (r, a, b, c) in enumerate(jobs):
+        arr[i].ring = r.h.value
+        arr[i].d_a = _ptr(a)
+        arr[i].d_b = _ptr(b)
+        arr[i].d_c = _ptr(c)
+    check(lib().cy_polymul_batched(arr, len(jobs), _stream_handle(stream)), "cy_polymul_batched")
+
+
+class Yashe:
+    """YASHE over Z_q[x]/(x^N+1) on the GPU (handle to a ``cy_yashe``)."""
+
+    def __init__(self, n: int, q: int, t: int, w_bits: int = 32, sigma: float = 8.0):
+        self.n, self.q, self.t, self.w_bits, self.sigma = n, q, t, w_bits, sigma
+        self.L = nlimbs(q)
+        self._qarr = limbs_of(q, self.L)
+        p = YasheParams(n=n, q=ctypes.cast(self._qarr, ctypes.POINTER(ctypes.c_uint64)), q_limbs=self.L, t=t,
+                        w_bits=w_bits, sigma=sigma)
+        h = ctypes.c_void_p()
+        check(lib().cy_yashe_create(ctypes.byref(p), ctypes.byref(h)), "cy_yashe_create")
+        self.h = h
+        rh = ctypes.c_void_p()
+        check(lib().cy_yashe_get_ring(h, ctypes.byref(rh)), "cy_yashe_get_ring")
+        self.ring = Ring(n, q, handle=rh, owner=self)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().cy_yashe_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def info(self) -> YasheInfo:
+        i = YasheInfo()
+        check(lib().cy_yashe_get_info(self.h, ctypes.byref(i)), "cy_yashe_get_info")
+        return i
+
+    @property
+    def ell(self) -> int:
+        return self.info().ell
+
+    def keygen(self, seed: int) -> None:
+        check(lib().cy_yashe_keygen(self.h, seed), "cy_yashe_keygen")
+
+    def set_keys(self, f, h, evk) -> None:
+        F = to_limb_array(f, self.L) if not isinstance(f, np.ndarray) else np.ascontiguousarray(f, np.uint64)
+        H = to_limb_array(h, self.L) if not isinstance(h, np.ndarray) else np.ascontiguousarray(h, np.uint64)
+        EV = to_limb_array(evk, self.L) if not isinstance(evk, np.ndarray) else np.ascontiguousarray(evk, np.uint64)
+        check(lib().cy_yashe_set_keys(self.h, F.ctypes.data, H.ctypes.data, EV.ctypes.data), "cy_yashe_set_keys")
+
+    def get_keys(self):
+        F = np.zeros((self.n, self.L), np.uint64)
+        H = np.zeros((self.n, self.L), np.uint64)
+        EV = np.zeros((self.ell, self.n, self.L), np.uint64)
+        check(lib().cy_yashe_get_keys(self.h, F.ctypes.data, H.ctypes.data, EV.ctypes.data), "cy_yashe_get_keys")
+        return F, H, EV
+
+    def encrypt_host(self, m: np.ndarray, seed: int) -> np.ndarray:
+        m = np.ascontiguousarray(m, dtype=np.uint64)
+        if m.ndim == 1:
+            m = m[None]
+        ct = np.zeros((m.shape[0], self.n, self.L), np.uint64)
+        check(lib().cy_yashe_encrypt_host(self.h, m.ctypes.data, ct.ctypes.data, m.shape[0], seed),
+              "cy_yashe_encrypt_host")
+        return ct
+
+    def decrypt(self, ct, aftermul: bool = False, stream=None):
+        import torch
+        out = torch.empty((ct.shape[0], self.n), dtype=torch.int64, device=ct.device)
+        check(lib().cy_yashe_decrypt(self.h, _ptr(ct), _ptr(out), ct.shape[0], 1 if aftermul else 0,
+                                     _stream_handle(stream)), "cy_yashe_decrypt")
+        return out
+
+    def mul(self, c1, c2, relin: bool = True, out=None, stream=None, workspace: Optional[Workspace] = None):
+        out = self.ring.empty(c1.shape[0]) if out is None else out
+        st = _stream_handle(stream)
+        if workspace is None:
+            check(lib().cy_yashe_mul(self.h, _ptr(c1), _ptr(c2), _ptr(out), c1.shape[0], 1 if relin else 0, st),
+                  "cy_yashe_mul")
+        else:
+            check(lib().cy_yashe_mul_ws(self.h, workspace.h, _ptr(c1), _ptr(c2), _ptr(out), c1.shape[0],
+                                        1 if relin else 0, st), "cy_yashe_mul_ws")
+        return out
+
+    def keyswitch(self, c, out=None, stream=None):
+        out = self.ring.empty(c.shape[0]) if out is None else out
+        check(lib().cy_yashe_keyswitch(self.h, _ptr(c), _ptr(out), c.shape[0], _stream_handle(stream)),
+              "cy_yashe_keyswitch")
+        return out
+
+    def add(self, c1, c2, out=None, stream=None):
+        out = self.ring.empty(c1.shape[0]) if out is None else out
+        check(lib().cy_yashe_add(self.h, _ptr(c1), _ptr(c2), _ptr(out), c1.shape[0], _stream_handle(stream)),
+              "cy_yashe_add")
+        return out
+
+
+__all__ = ["Ring", "Yashe", "Workspace", "polymul_batched", "to_limb_array", "from_limb_array", "to_device",
+           "to_host", "nlimbs", "CY_OK"]

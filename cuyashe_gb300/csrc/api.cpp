@@ -1,0 +1,435 @@
+// api.cpp -- the extern "C" boundary (include/cuyashe.h).
+//
+// Launch sequence of one product batch, per chunk of jobs:
+//   k_mul / k_keyswitch  grid (k primes, jobs)  -> residues in the workspace
+//   k_epi                grid (jobs * N / 256)  -> limbs (or plaintext words)
+// all on the caller's stream, no host synchronisation, no allocation once the
+// workspace has grown to the chunk size. The reference allocates 4 residue
+// buffers per product and synchronises the device after every operation
+// (src/cuda_functions.cu:670-738, src/common.h:223).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <set>
+#include <utility>
+
+#include "host.h"
+
+namespace cy {
+
+const char* last_error_message();
+void* addsub_kernel(int l64, bool sub);
+void* crt_kernel();
+void* shoup_pairs_kernel();
+
+static constexpr int kEpiThreads = 256;
+
+static int default_chunk(int n) {
+    // jobs per launch: keep the residue scratch of a chunk around 32 MiB so it
+    // stays resident in L2 between the NTT kernel and the epilogue
+    long long per_job = (long long)n * 27 * 4;
+    long long c = (32ll << 20) / per_job;
+    if (c < 1) c = 1;
+    if (c > 4096) c = 4096;
+    return (int)c;
+}
+
+static cy_status ensure_smem(void* func, size_t bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<void*, int>> done;
+    int dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({func, dev})) return CY_OK;
+    if (bytes > 48 * 1024) CY_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    done.insert({func, dev});
+    return CY_OK;
+}
+
+static cy_status launch(void* func, dim3 grid, dim3 block, size_t smem, cudaStream_t st, void** args) {
+    if (!func) return set_error(CY_ERR_INTERNAL, "missing kernel instantiation");
+    CY_TRY(ensure_smem(func, smem));
+    CY_CUDA(cudaLaunchKernel(func, grid, block, args, smem, st));
+    return CY_OK;
+}
+
+static cy_status check_device(int device) {
+    int cur = -1;
+    CY_CUDA(cudaGetDevice(&cur));
+    if (cur != device) return set_error(CY_ERR_INVALID_ARGUMENT, "handle belongs to another CUDA device");
+    return CY_OK;
+}
+
+// products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j)
+static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, long long a_stride,
+                             const uint64_t* b, long long b_stride, void* out, long long out_stride, int batch,
+                             Workspace& ws, cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    const KernelSet& ks = kernel_set(B.h.logn);
+    const int n = B.h.n, k = B.h.k;
+    const int chunk = std::min(batch, default_chunk(n));
+    CY_TRY(ws.reserve((size_t)chunk * k * n));
+    void* epi = epi_kernel(B.h.l32, B.h.mode);
+    for (int j0 = 0; j0 < batch; j0 += chunk) {
+        int nj = std::min(chunk, batch - j0);
+        const uint64_t* aj = a + (size_t)j0 * a_stride;
+        const uint64_t* bj = b + (size_t)j0 * b_stride;
+        const BasisDev* Bd = B.d;
+        uint32_t* resid = ws.d_resid;
+        void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
+        CY_TRY(launch(ks.mul[centered ? 1 : 0], dim3(k, nj), dim3(ks.threads), ks.smem_mul, st, args));
+        void* oj = (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t);
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        long long threads = (long long)nj * n;
+        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
+                      eargs));
+    }
+    return CY_OK;
+}
+
+// keyswitch of `batch` polynomials c_j -> out_j (may alias c)
+static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out,
+                               int batch, Workspace& ws, cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    const KernelSet& ks = kernel_set(B.h.logn);
+    const int n = B.h.n, k = B.h.k, l64 = B.h.l64;
+    const int chunk = std::min(batch, default_chunk(n));
+    CY_TRY(ws.reserve((size_t)chunk * k * n));
+    int maxsm = 0, dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    CY_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int sel = (ell % 4 == 0 && ks.smem_ks[1] <= (size_t)maxsm) ? 1 : 0;
+    void* epi = epi_kernel(B.h.l32, B.h.mode);
+    for (int j0 = 0; j0 < batch; j0 += chunk) {
+        int nj = std::min(chunk, batch - j0);
+        const uint64_t* cj = c + (size_t)j0 * n * l64;
+        const BasisDev* Bd = B.d;
+        uint32_t* resid = ws.d_resid;
+        void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
+        CY_TRY(launch(ks.ks[sel], dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel], st, args));
+        uint64_t* oj = out + (size_t)j0 * n * l64;
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        long long threads = (long long)nj * n;
+        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
+                      eargs));
+    }
+    return CY_OK;
+}
+
+static cy_status run_crt(const Basis& B, const uint64_t* x, uint32_t* res, const uint32_t* d_scale, int batch,
+                         cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    const BasisDev* Bd = B.d;
+    long long threads = (long long)batch * B.h.n;
+    void* args[] = {(void*)&Bd, (void*)&x, (void*)&res, (void*)&d_scale, (void*)&batch};
+    return launch(crt_kernel(), dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st, args);
+}
+
+static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    const KernelSet& ks = kernel_set(B.h.logn);
+    const BasisDev* Bd = B.d;
+    const uint32_t* ninv = B.d_ninv;
+    void* args[] = {(void*)&Bd, (void*)&res, (void*)&ninv};
+    for (int j0 = 0; j0 < batch; j0 += 65535) {
+        int nj = std::min(65535, batch - j0);
+        uint32_t* rj = res + (size_t)j0 * B.h.k * B.h.n;
+        args[1] = (void*)&rj;
+        CY_TRY(launch(ks.ntt[inverse ? 1 : 0], dim3(B.h.k, nj), dim3(ks.threads), ks.smem_ntt, st, args));
+    }
+    return CY_OK;
+}
+
+static cy_status run_addsub(const cy_ring* r, const uint64_t* a, const uint64_t* b, uint64_t* c, int batch, bool sub,
+                            cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    long long count = (long long)batch * r->n;
+    const uint64_t* q = r->d_q;
+    void* args[] = {(void*)&a, (void*)&b, (void*)&c, (void*)&q, (void*)&count};
+    return launch(addsub_kernel(r->l64, sub), dim3((unsigned)((count + 255) / 256)), dim3(256), 0, st, args);
+}
+
+static cy_status validate_poly_args(const cy_ring* r, const void* a, const void* b, const void* c, int batch) {
+    if (!r) return set_error(CY_ERR_INVALID_ARGUMENT, "ring is NULL");
+    if (batch < 0) return set_error(CY_ERR_INVALID_ARGUMENT, "batch < 0");
+    if (batch > 0 && (!a || !b || !c)) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL buffer");
+    return check_device(r->device);
+}
+
+// bound = 4 * N * q^2: |X| < N q^2 for products of values in [0, q)
+static BigUInt product_bound(int n, const BigUInt& q) { return BigUInt(4ull * (uint64_t)n) * q * q; }
+
+cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
+                          long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
+                          cudaStream_t st) {
+    return run_product(B, centered, a, a_stride, b, b_stride, out, out_stride, batch, ws, st);
+}
+
+cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
+                            Workspace& ws, cudaStream_t st) {
+    return run_keyswitch(B, c, evk, ell, out, batch, ws, st);
+}
+
+// Evaluation key in the keyswitch basis, NTT domain, with Shoup companions:
+// d_evk [ell][k][N] of (value, floor(value 2^32 / p)). Synchronous.
+cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk) {
+    const int k = relin.h.k;
+    const size_t words = (size_t)ell * k * n;
+    uint64_t* d_limbs = nullptr;
+    uint32_t* d_res = nullptr;
+    uint2* out = nullptr;
+    cudaError_t e = cudaMalloc(&d_limbs, sizeof(uint64_t) * (size_t)ell * n * l64);
+    if (e == cudaSuccess) e = cudaMalloc(&d_res, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(uint2) * words);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_limbs, h_evk, sizeof(uint64_t) * (size_t)ell * n * l64, cudaMemcpyHostToDevice);
+    cy_status st = (e == cudaSuccess) ? CY_OK : cuda_error(e, "evaluation key upload");
+    if (st == CY_OK) st = run_crt(relin, d_limbs, d_res, nullptr, ell, 0);
+    if (st == CY_OK) st = run_ntt(relin, d_res, ell, false, 0);
+    if (st == CY_OK) {
+        const BasisDev* Bd = relin.d;
+        long long total = (long long)words;
+        void* args[] = {(void*)&Bd, (void*)&d_res, (void*)&out, (void*)&total};
+        st = launch(shoup_pairs_kernel(), dim3((unsigned)((total + 255) / 256)), dim3(256), 0, 0, args);
+    }
+    if (st == CY_OK) {
+        e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = cuda_error(e, "evaluation key transform");
+    }
+    cudaFree(d_limbs);
+    cudaFree(d_res);
+    if (st != CY_OK) {
+        cudaFree(out);
+        return st;
+    }
+    *d_evk = out;
+    return CY_OK;
+}
+
+}  // namespace cy
+
+using namespace cy;
+
+// ---- rings ----------------------------------------------------------------------
+cy_ring::~cy_ring() {
+    if (d_q) cudaFree(d_q);
+}
+
+extern "C" {
+
+const char* cy_status_string(int status) {
+    switch (status) {
+        case CY_OK: return "ok";
+        case CY_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case CY_ERR_UNSUPPORTED: return "unsupported parameters";
+        case CY_ERR_CUDA: return "CUDA error";
+        case CY_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case CY_ERR_NOT_INVERTIBLE: return "not invertible";
+        case CY_ERR_NO_KEYS: return "no keys";
+        case CY_ERR_TIMEOUT: return "timeout";
+        case CY_ERR_BUSY: return "busy";
+        case CY_ERR_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+const char* cy_last_error(void) { return last_error_message(); }
+
+int cy_version(void) { return 1; }
+
+cy_status cy_ring_create(int n, const uint64_t* h_q, int q_limbs, cy_ring** out) {
+    if (!out || !h_q) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (n < 2 || n > NMAX || (n & (n - 1))) return set_error(CY_ERR_UNSUPPORTED, "N must be a power of two in [2, 16384]");
+    if (q_limbs < 1 || q_limbs > 6) return set_error(CY_ERR_UNSUPPORTED, "q_limbs must be 1..6");
+    BigUInt q = BigUInt::from_limbs64(h_q, q_limbs);
+    if (q.bits() < 2) return set_error(CY_ERR_INVALID_ARGUMENT, "q must be >= 2");
+    if (q.bits() > 64 * q_limbs) return set_error(CY_ERR_INTERNAL, "limb conversion");
+    int dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    std::unique_ptr<cy_ring> r(new cy_ring());
+    r->device = dev;
+    r->n = n;
+    while ((1 << r->logn) < n) r->logn++;
+    r->q = q;
+    r->qbits = q.bits();
+    r->l32 = (r->qbits + 31) / 32;
+    r->l64 = (r->qbits + 63) / 64;
+    r->q_limbs.assign(r->l64, 0);
+    q.to_limbs64(r->q_limbs.data(), r->l64);
+    CY_TRY(build_basis(r->mul, dev, n, q, EPI_MODQ, product_bound(n, q), 0, true, true, false));
+    CY_TRY(build_basis(r->plain, dev, n, q, EPI_MODQ, product_bound(n, q), 0, false, false, false));
+    CY_CUDA(cudaMalloc(&r->d_q, sizeof(uint64_t) * r->l64));
+    CY_CUDA(cudaMemcpy(r->d_q, r->q_limbs.data(), sizeof(uint64_t) * r->l64, cudaMemcpyHostToDevice));
+    r->own_ws.ws.device = dev;
+    *out = r.release();
+    return CY_OK;
+}
+
+cy_status cy_ring_destroy(cy_ring* ring) {
+    delete ring;
+    return CY_OK;
+}
+
+cy_status cy_ring_get_info(const cy_ring* r, cy_ring_info* info) {
+    if (!r || !info) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(info, 0, sizeof(*info));
+    info->n = r->n;
+    info->q_limbs = r->l64;
+    info->q_bits = r->qbits;
+    info->crt_primes = r->mul.h.k;
+    info->crt_bits = r->mul.crt_bits;
+    for (int i = 0; i < r->mul.h.k; i++) info->primes[i] = r->mul.h.p[i];
+    return CY_OK;
+}
+
+cy_status cy_workspace_create(cy_workspace** out) {
+    if (!out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = new cy_workspace();
+    CY_CUDA(cudaGetDevice(&(*out)->ws.device));
+    return CY_OK;
+}
+
+cy_status cy_workspace_destroy(cy_workspace* ws) {
+    delete ws;
+    return CY_OK;
+}
+
+cy_status cy_polymul_ws(cy_ring* r, cy_workspace* ws, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_c,
+                        int batch, cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_a, d_b, d_c, batch));
+    const long long stride = (long long)r->n * r->l64;
+    if (!ws) {
+        std::lock_guard<std::mutex> lock(r->mu);
+        return run_product(r->mul, false, d_a, stride, d_b, stride, d_c, stride, batch, r->own_ws.ws,
+                           (cudaStream_t)stream);
+    }
+    return run_product(r->mul, false, d_a, stride, d_b, stride, d_c, stride, batch, ws->ws, (cudaStream_t)stream);
+}
+
+cy_status cy_polymul(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_c, int batch,
+                     cy_stream_t stream) {
+    return cy_polymul_ws(r, nullptr, d_a, d_b, d_c, batch, stream);
+}
+
+cy_status cy_polymul_host(cy_ring* r, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_c, int batch) {
+    CY_TRY(validate_poly_args(r, h_a, h_b, h_c, batch));
+    if (batch == 0) return CY_OK;
+    const size_t bytes = sizeof(uint64_t) * (size_t)batch * r->n * r->l64;
+    uint64_t *a = nullptr, *b = nullptr, *c = nullptr;
+    cudaError_t e = cudaMalloc(&a, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c, bytes);
+    cy_status st = CY_OK;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a, h_a, bytes, cudaMemcpyHostToDevice, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b, h_b, bytes, cudaMemcpyHostToDevice, 0);
+    if (e == cudaSuccess) st = cy_polymul(r, a, b, c, batch, 0);
+    if (e == cudaSuccess && st == CY_OK) e = cudaMemcpyAsync(h_c, c, bytes, cudaMemcpyDeviceToHost, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    cudaFree(a);
+    cudaFree(b);
+    cudaFree(c);
+    if (e != cudaSuccess) return cuda_error(e, "cy_polymul_host");
+    return st;
+}
+
+cy_status cy_polyadd(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_c, int batch,
+                     cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_a, d_b, d_c, batch));
+    return run_addsub(r, d_a, d_b, d_c, batch, false, (cudaStream_t)stream);
+}
+
+cy_status cy_polysub(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_c, int batch,
+                     cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_a, d_b, d_c, batch));
+    return run_addsub(r, d_a, d_b, d_c, batch, true, (cudaStream_t)stream);
+}
+
+cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_scalar, uint64_t* d_c, int batch,
+                             cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_a, h_scalar, d_c, batch));
+    if (batch == 0) return CY_OK;
+    BigUInt s = BigUInt::from_limbs64(h_scalar, r->l64);
+    if (s >= r->q) return set_error(CY_ERR_INVALID_ARGUMENT, "scalar must be < q");
+    std::lock_guard<std::mutex> lock(r->mu);
+    const Basis& B = r->plain;
+    const int k = B.h.k, n = r->n;
+    // residues of a times (s mod p_i), then the plain ICRT epilogue: |a s| < q^2 < M/4
+    std::vector<uint32_t> scale(2 * (size_t)k);
+    for (int i = 0; i < k; i++) {
+        const uint32_t p = B.h.p[i], v = s.mod_u32(p);
+        scale[2 * i] = v;
+        scale[2 * i + 1] = (uint32_t)(((uint64_t)v << 32) / p);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int chunk = std::min(batch, default_chunk(n));
+    Workspace& ws = r->own_ws.ws;
+    CY_TRY(ws.reserve((size_t)chunk * k * n + 2 * (size_t)KMAX));
+    uint32_t* d_scale = ws.d_resid + (size_t)chunk * k * n;
+    CY_CUDA(cudaMemcpyAsync(d_scale, scale.data(), sizeof(uint32_t) * scale.size(), cudaMemcpyHostToDevice, st));
+    void* epi = epi_kernel(B.h.l32, EPI_MODQ);
+    for (int j0 = 0; j0 < batch; j0 += chunk) {
+        int nj = std::min(chunk, batch - j0);
+        const uint64_t* aj = d_a + (size_t)j0 * n * r->l64;
+        CY_TRY(run_crt(B, aj, ws.d_resid, d_scale, nj, st));
+        const BasisDev* Bd = B.d;
+        uint32_t* resid = ws.d_resid;
+        uint64_t* oj = d_c + (size_t)j0 * n * r->l64;
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        long long threads = (long long)nj * n;
+        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
+                      eargs));
+    }
+    // the scale vector is read by the kernels above before the stream moves on
+    return CY_OK;
+}
+
+cy_status cy_polymul_batched(const cy_polymul_job* jobs, int njobs, cy_stream_t stream) {
+    if (njobs < 0 || (njobs > 0 && !jobs)) return set_error(CY_ERR_INVALID_ARGUMENT, "bad job list");
+    // group consecutive jobs of the same ring whose buffers are contiguous
+    int i = 0;
+    while (i < njobs) {
+        cy_ring* r = jobs[i].ring;
+        CY_TRY(validate_poly_args(r, jobs[i].d_a, jobs[i].d_b, jobs[i].d_c, 1));
+        const long long stride = (long long)r->n * r->l64;
+        int j = i + 1;
+        while (j < njobs && jobs[j].ring == r && jobs[j].d_a == jobs[i].d_a + (j - i) * stride &&
+               jobs[j].d_b == jobs[i].d_b + (j - i) * stride && jobs[j].d_c == jobs[i].d_c + (j - i) * stride)
+            j++;
+        CY_TRY(cy_polymul(r, jobs[i].d_a, jobs[i].d_b, jobs[i].d_c, j - i, stream));
+        i = j;
+    }
+    return CY_OK;
+}
+
+cy_status cy_ntt(cy_ring* r, uint32_t* d_res, int batch, int inverse, cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_res, d_res, d_res, batch));
+    return run_ntt(r->plain, d_res, batch, inverse != 0, (cudaStream_t)stream);
+}
+
+cy_status cy_crt(cy_ring* r, const uint64_t* d_x, uint32_t* d_res, int batch, cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_x, d_res, d_res, batch));
+    return run_crt(r->plain, d_x, d_res, nullptr, batch, (cudaStream_t)stream);
+}
+
+cy_status cy_icrt(cy_ring* r, const uint32_t* d_res, uint64_t* d_x, int batch, cy_stream_t stream) {
+    CY_TRY(validate_poly_args(r, d_res, d_x, d_x, batch));
+    if (batch == 0) return CY_OK;
+    const Basis& B = r->plain;
+    const BasisDev* Bd = B.d;
+    void* epi = epi_kernel(B.h.l32, EPI_MODQ);
+    for (int j0 = 0; j0 < batch; j0 += 65536) {
+        int nj = std::min(65536, batch - j0);
+        const uint32_t* rj = d_res + (size_t)j0 * B.h.k * r->n;
+        uint64_t* xj = d_x + (size_t)j0 * r->n * r->l64;
+        void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj};
+        long long threads = (long long)nj * r->n;
+        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0,
+                      (cudaStream_t)stream, eargs));
+    }
+    return CY_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// arith.cuh -- 32-bit modular arithmetic for word-sized NTT primes p < 2^30.
+//
+// The reference reduces modulo one 64-bit Goldilocks prime with __umul64hi and a
+// three-case fix-up (s_mul, src/cuda_functions.cu:310-349), i.e. emulated
+// 64x64-bit products on every butterfly. Here every residue is a 32-bit word
+// and products are 32x32-bit:
+//   * Shoup multiplication by a precomputed constant (twiddles, CRT factors):
+//     one mul.hi and two mul.lo, result in [0, 2p) for any 32-bit input;
+//   * Montgomery multiplication for the pointwise product of two variables;
+//   * lazy reduction with the unsigned-min trick min(x, x - m).
+#pragma once
+
+#include <stdint.h>
+
+namespace cy {
+
+__device__ __forceinline__ uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+
+// x in [0, 2m) -> [0, m)   (x - m wraps above x when x < m)
+__device__ __forceinline__ uint32_t red(uint32_t x, uint32_t m) { return umin32(x, x - m); }
+
+// x * w mod p in [0, 2p), any 32-bit x; w < p, ws = floor(w * 2^32 / p), p < 2^31.
+__device__ __forceinline__ uint32_t shoup(uint32_t x, uint32_t w, uint32_t ws, uint32_t p) {
+    const uint32_t q = __umulhi(x, ws);
+    return x * w - q * p;
+}
+
+// a * b * 2^-32 mod p in [0, 2p) for a, b in [0, 2p), p < 2^30; pinv = -p^-1 mod 2^32.
+__device__ __forceinline__ uint32_t mont(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    const uint64_t T = (uint64_t)a * b;
+    const uint32_t m = (uint32_t)T * pinv;
+    const uint64_t u = T + (uint64_t)m * p;  // low word is zero
+    return (uint32_t)(u >> 32);
+}
+
+// Cooley-Tukey butterfly (Harvey's lazy form): X, Y in [0, 4p) -> X + wY, X - wY in [0, 4p).
+__device__ __forceinline__ void ct_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, uint32_t p) {
+    const uint32_t p2 = 2 * p;
+    const uint32_t x = red(X, p2);
+    const uint32_t t = shoup(Y, w, ws, p);
+    Y = x - t + p2;
+    X = x + t;
+}
+
+// Gentleman-Sande butterfly: X, Y in [0, 2p) -> X + Y, (X - Y) w in [0, 2p).
+__device__ __forceinline__ void gs_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, uint32_t p) {
+    const uint32_t p2 = 2 * p;
+    const uint32_t s = red(X + Y, p2);
+    const uint32_t d = X - Y + p2;
+    Y = shoup(d, w, ws, p);
+    X = s;
+}
+
+}  // namespace cy

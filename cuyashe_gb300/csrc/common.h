@@ -1,0 +1,54 @@
+// common.h -- definitions shared by the host set-up code and the CUDA kernels.
+#pragma once
+
+#include <stdint.h>
+#include <vector_types.h>
+
+namespace cy {
+
+constexpr int KMAX = 40;          // primes per CRT basis
+constexpr int L32MAX = 12;        // 32-bit words of q (384 bits)
+constexpr int LOGN_MAX = 14;      // N <= 16384
+constexpr int NMAX = 1 << LOGN_MAX;
+constexpr int TABLE_PRIMES = 64;  // word-sized NTT primes with device twiddle tables
+constexpr int PRIME_TWO_ADIC = 16;  // every table prime is 1 mod 2^16
+
+// What the epilogue of a product kernel computes from the recombined integer X
+// (|X| < M/4, M the basis product):
+//   MODQ     X mod q                                  -> [N][L] limbs
+//   YASHE    round(t*X/q) mod q                       -> [N][L] limbs
+//   DECRYPT  round(t*(X mod q)/q) mod t               -> [N] uint64
+enum EpiMode { EPI_MODQ = 0, EPI_YASHE = 1, EPI_DECRYPT = 2 };
+
+// Constants of one CRT basis for one ring (N, q). Lives in device memory; the
+// kernels read the per-prime fields of their own prime and the epilogue copies
+// what it needs into shared memory.
+//
+// Notation: p_i the basis primes, M = prod p_i, Mhat_i = M/p_i, s = 32*l32 -
+// bits(q) the normalising shift so that q' = q << s has its top bit set.
+struct BasisDev {
+    int n, logn, k, l32, l64, mode, shift, qbits;
+    uint32_t t;        // plaintext modulus (YASHE / DECRYPT)
+    uint32_t centered; // inputs are taken as symmetric representatives (YASHE)
+    uint64_t mu;       // floor(2^(32*l32+37) / q')
+    uint32_t qn[L32MAX];       // q'
+    uint32_t q[L32MAX];        // q
+    uint32_t qhalf[L32MAX];    // (q-1)/2
+    uint32_t qhalf_n[L32MAX];  // ((q-1)/2) << s
+    uint32_t B0[L32MAX];       // MODQ: ((-M) mod q) << s        YASHE: ((-I_M) mod q) << s
+    uint32_t B1[L32MAX];       //                                YASHE: (q - R_M) << s
+    uint32_t p[KMAX];
+    uint32_t pinv[KMAX];       // -p^-1 mod 2^32
+    uint32_t ycon[KMAX];       // residue -> [X * Mhat_i^-1]_{p_i} factor (N^-1, Montgomery folded)
+    uint32_t ycon_sh[KMAX];    // Shoup companion of ycon
+    uint32_t flo[KMAX], fhi[KMAX];  // floor(2^64/p_i) split in words (estimate of X'/M)
+    uint32_t qmodp[KMAX];      // q mod p_i (centering)
+    uint32_t r32[KMAX], r32_sh[KMAX];  // 2^32 mod p_i with Shoup companion
+    uint32_t crt[KMAX][L32MAX];        // 2^(32 j) mod p_i
+    uint32_t A0[KMAX][L32MAX];  // MODQ: (Mhat_i mod q) << s     YASHE: (I_i mod q) << s, t*Mhat_i = I_i q + R_i
+    uint32_t A1[KMAX][L32MAX];  //                                YASHE: R_i << s
+    const uint2* psi[KMAX];     // forward twiddles (w, floor(w 2^32/p)), bit-reversed powers of psi
+    const uint2* ipsi[KMAX];    // inverse twiddles
+};
+
+}  // namespace cy

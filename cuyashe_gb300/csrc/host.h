@@ -1,0 +1,110 @@
+// host.h -- internal host-side objects behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cuyashe.h"
+#include "bigint.h"
+#include "common.h"
+#include "dispatch.h"
+
+namespace cy {
+
+// ---- errors ---------------------------------------------------------------
+cy_status set_error(cy_status st, const std::string& msg);
+cy_status cuda_error(cudaError_t e, const char* what);
+#define CY_CUDA(call)                                          \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return cy::cuda_error(_e, #call); \
+    } while (0)
+#define CY_TRY(call)                    \
+    do {                                \
+        cy_status _s = (call);          \
+        if (_s != CY_OK) return _s;     \
+    } while (0)
+
+// ---- word-sized NTT primes with device twiddle tables ----------------------
+// The TABLE_PRIMES largest primes p < 2^30 with p = 1 (mod 2^16), descending.
+// For each, psi is a primitive 2^(LOGN_MAX+1)-th root of unity; the forward
+// table holds psi^bitrev(i) and the inverse table psi^-bitrev(i) (bit reversal
+// over LOGN_MAX bits) with Shoup companions. A prefix of length N of these
+// tables is the table of the length-N transform (psi_N = psi^(NMAX/N)).
+struct PrimeTable {
+    int device = -1;
+    std::vector<uint32_t> primes;
+    uint2* d_psi = nullptr;   // [TABLE_PRIMES][NMAX]
+    uint2* d_ipsi = nullptr;  // [TABLE_PRIMES][NMAX]
+};
+cy_status prime_table(int device, const PrimeTable** out);
+const std::vector<uint32_t>& table_primes();  // host-only, no CUDA
+
+// ---- a CRT basis for one ring and one epilogue ------------------------------
+struct Basis {
+    BasisDev h{};
+    BasisDev* d = nullptr;
+    uint32_t* d_ninv = nullptr;  // [k][2]: N^-1 mod p_i and its Shoup companion
+    int crt_bits = 0;
+    Basis() = default;
+    Basis(const Basis&) = delete;
+    Basis& operator=(const Basis&) = delete;
+    ~Basis();
+};
+
+// Host constants only (no device memory): smallest prefix of the table primes
+// whose product exceeds `bound`.
+// `scale_n` folds N^-1 (inverse NTT without scaling) and `mont` folds 2^32
+// (Montgomery pointwise product) into the residue factors of the epilogue.
+cy_status basis_constants(BasisDev& h, int* crt_bits, int n, const BigUInt& q, int mode, const BigUInt& bound,
+                          uint32_t t, bool mont, bool scale_n, bool centered);
+cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, const BigUInt& bound, uint32_t t,
+                      bool mont, bool scale_n, bool centered);
+
+// ---- scratch ------------------------------------------------------------------
+struct Workspace {
+    int device = -1;
+    uint32_t* d_resid = nullptr;
+    size_t resid_words = 0;
+    cy_status reserve(size_t words);
+    ~Workspace();
+};
+
+}  // namespace cy
+
+struct cy_workspace {
+    cy::Workspace ws;
+};
+
+struct cy_ring {
+    int device = -1;
+    int n = 0, logn = 0, l64 = 0, l32 = 0, qbits = 0;
+    cy::BigUInt q;
+    std::vector<uint64_t> q_limbs;
+    uint64_t* d_q = nullptr;   // q as l64 limbs (elementwise kernels)
+    cy::Basis mul;             // product basis, mod-q epilogue (N^-1 and 2^32 folded)
+    cy::Basis plain;           // same primes, plain residues (ICRT, scalar multiply, NTT)
+    cy_workspace own_ws;
+    std::mutex mu;
+    ~cy_ring();
+};
+
+struct cy_yashe {
+    cy_ring* ring = nullptr;
+    uint64_t t = 0;
+    int w_bits = 32, ell = 0;
+    double sigma = 8.0;
+    cy::Basis tensor;  // centered inputs, round(t/q .) epilogue
+    cy::Basis relin;   // keyswitch basis, mod-q epilogue
+    cy::Basis dec;     // key * ciphertext, decryption epilogue
+    bool has_keys = false;
+    std::vector<uint64_t> h_f, h_h, h_evk;
+    uint64_t* d_f = nullptr;
+    uint64_t* d_f2 = nullptr;
+    uint2* d_evk = nullptr;  // [ell][k'][N] NTT-domain evaluation key
+    ~cy_yashe();
+};

@@ -1,0 +1,147 @@
+// ICRT epilogues, CRT split, elementwise mod-q kernels and the dispatch tables.
+#include <mutex>
+
+#include "kernels.cuh"
+
+namespace cy {
+
+void fill_small(KernelSet* t);
+void fill_n10_11(KernelSet* t);
+void fill_n12(KernelSet* t);
+void fill_n13(KernelSet* t);
+void fill_n14(KernelSet* t);
+
+const KernelSet& kernel_set(int logn) {
+    static KernelSet table[LOGN_MAX + 1];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        fill_small(table);
+        fill_n10_11(table);
+        fill_n12(table);
+        fill_n13(table);
+        fill_n14(table);
+    });
+    return table[logn];
+}
+
+#define CY_EPI_ROW(L) {(void*)k_epi<L, EPI_MODQ>, (void*)k_epi<L, EPI_YASHE>, (void*)k_epi<L, EPI_DECRYPT>}
+
+void* epi_kernel(int l32, int mode) {
+    static void* table[L32MAX + 1][3] = {
+        {nullptr, nullptr, nullptr}, CY_EPI_ROW(1), CY_EPI_ROW(2), CY_EPI_ROW(3), CY_EPI_ROW(4),
+        CY_EPI_ROW(5),  CY_EPI_ROW(6), CY_EPI_ROW(7), CY_EPI_ROW(8), CY_EPI_ROW(9), CY_EPI_ROW(10),
+        CY_EPI_ROW(11), CY_EPI_ROW(12)};
+    if (l32 < 1 || l32 > L32MAX || mode < 0 || mode > 2) return nullptr;
+    return table[l32][mode];
+}
+
+// Residues [job][k][N] in [0, p) of limbs [job][N][l64]; each residue is also
+// multiplied by scale[i] (value, Shoup companion) when `scale` is not null.
+__global__ void k_crt(const BasisDev* __restrict__ B, const uint64_t* __restrict__ X, uint32_t* __restrict__ res,
+                      const uint32_t* __restrict__ scale, int njobs) {
+    __shared__ uint32_t s_crt[KMAX * L32MAX];
+    const int k = B->k, logn = B->logn, l64 = B->l64;
+    for (int i = threadIdx.x; i < k * L32MAX; i += blockDim.x) s_crt[i] = B->crt[i / L32MAX][i % L32MAX];
+    __syncthreads();
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = 1 << logn;
+    const long long job = idx >> logn;
+    if (job >= njobs) return;
+    const int coef = (int)(idx & (n - 1));
+    const uint64_t* x = X + (size_t)job * n * l64;
+    for (int i = 0; i < k; i++) {
+        const PrimeCtx c = load_prime_ctx(B, i);
+        uint32_t r = crt_coef<false>(x, coef, l64, &s_crt[i * L32MAX], nullptr, c);
+        if (scale) r = shoup(r, scale[2 * i], scale[2 * i + 1], c.p);
+        r = red(red(r, 2 * c.p), c.p);
+        res[((size_t)job * k + i) * n + coef] = r;
+    }
+}
+
+// Shoup companions of NTT-domain values: out[j] = (v, floor(v 2^32 / p_i)) for
+// the residue vectors of a [ell][k][N] array.
+__global__ void k_shoup_pairs(const BasisDev* __restrict__ B, const uint32_t* __restrict__ v, uint2* __restrict__ out,
+                              long long total) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int n = 1 << B->logn;
+    const int prime = (int)((idx >> B->logn) % B->k);
+    (void)n;
+    const uint32_t p = B->p[prime];
+    const uint32_t x = v[idx];
+    out[idx] = make_uint2(x, (uint32_t)(((uint64_t)x << 32) / p));
+}
+
+// Elementwise c = a +/- b mod q over [count][l64] limbs (inputs in [0, q)).
+template <int L64, bool SUB>
+__global__ void k_addsub(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ c,
+                         const uint64_t* __restrict__ q, long long count) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    uint64_t x[L64], y[L64], s[L64], t[L64], qq[L64];
+#pragma unroll
+    for (int j = 0; j < L64; j++) {
+        x[j] = a[idx * L64 + j];
+        y[j] = b[idx * L64 + j];
+        qq[j] = q[j];
+    }
+    if (!SUB) {
+        // s = x + y; t = s - q; pick t unless it borrows (and s did not carry)
+        uint64_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < L64; j++) {
+            const uint64_t u = x[j] + y[j];
+            const uint64_t c1 = u < x[j];
+            s[j] = u + carry;
+            carry = c1 | (s[j] < u);
+        }
+        uint64_t br = 0;
+#pragma unroll
+        for (int j = 0; j < L64; j++) {
+            const uint64_t d = s[j] - qq[j];
+            const uint64_t b1 = s[j] < qq[j];
+            t[j] = d - br;
+            br = b1 | (d < br);
+        }
+        const bool use_t = carry || !br;
+#pragma unroll
+        for (int j = 0; j < L64; j++) c[idx * L64 + j] = use_t ? t[j] : s[j];
+    } else {
+        // s = x - y; if it borrows, add q
+        uint64_t br = 0;
+#pragma unroll
+        for (int j = 0; j < L64; j++) {
+            const uint64_t d = x[j] - y[j];
+            const uint64_t b1 = x[j] < y[j];
+            s[j] = d - br;
+            br = b1 | (d < br);
+        }
+        uint64_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < L64; j++) {
+            const uint64_t u = s[j] + qq[j];
+            const uint64_t c1 = u < s[j];
+            t[j] = u + carry;
+            carry = c1 | (t[j] < u);
+        }
+#pragma unroll
+        for (int j = 0; j < L64; j++) c[idx * L64 + j] = br ? t[j] : s[j];
+    }
+}
+
+void* addsub_kernel(int l64, bool sub) {
+    static void* table[7][2] = {{nullptr, nullptr},
+                                {(void*)k_addsub<1, false>, (void*)k_addsub<1, true>},
+                                {(void*)k_addsub<2, false>, (void*)k_addsub<2, true>},
+                                {(void*)k_addsub<3, false>, (void*)k_addsub<3, true>},
+                                {(void*)k_addsub<4, false>, (void*)k_addsub<4, true>},
+                                {(void*)k_addsub<5, false>, (void*)k_addsub<5, true>},
+                                {(void*)k_addsub<6, false>, (void*)k_addsub<6, true>}};
+    if (l64 < 1 || l64 > 6) return nullptr;
+    return table[l64][sub ? 1 : 0];
+}
+
+void* crt_kernel() { return (void*)k_crt; }
+void* shoup_pairs_kernel() { return (void*)k_shoup_pairs; }
+
+}  // namespace cy

@@ -1,0 +1,6 @@
+// Kernel instantiations for N = 16384.
+#include "kernels.cuh"
+
+namespace cy {
+void fill_n14(KernelSet* t) { fill_kernel_set<14, 4>(t[14]); }
+}  // namespace cy

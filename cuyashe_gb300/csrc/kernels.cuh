@@ -1,0 +1,444 @@
+// kernels.cuh -- CUDA kernels of the multiply path (templates; instantiated in
+// the k_*.cu translation units).
+//
+//   k_mul        per (job, prime): CRT split of a and b -> forward NTTs ->
+//                pointwise Montgomery product -> inverse NTT -> residues.
+//                Replaces callCRT (src/cuda_bn.cu:970-1002) and the NTT branch of
+//                callPolynomialMul (src/cuda_functions.cu:658-738).
+//   k_keyswitch  per (job, prime): base-2^32 digits of c -> forward NTTs ->
+//                sum_d D_d * evk_d in the NTT domain -> inverse NTT -> residues.
+//                Replaces Ciphertext::keyswitch (src/ciphertext.cpp:81-107).
+//   k_epi        per coefficient: ICRT of the k residues to the exact integer,
+//                then mod q, round(t/q .) or decryption. Replaces cuPreICRT /
+//                cuICRT / cuModN (src/cuda_bn.cu:759-968), Polynomial::reduce's
+//                mod q (src/cuda_functions.cu:1076) and the host rounding loop
+//                of Ciphertext::operator* (src/ciphertext.cpp:55-63).
+//   k_ntt, k_crt standalone transforms (callNTT, callCRT).
+#pragma once
+
+#include <stdint.h>
+
+#include "arith.cuh"
+#include "common.h"
+#include "dispatch.h"
+#include "ntt_core.cuh"
+
+namespace cy {
+
+// Exchange-region stride (words) for a kernel whose widest exchange carries
+// NOPS operands: two alternating regions when they fit, else one (stride 0).
+template <class PL, int NOPS>
+__host__ __device__ constexpr int region_stride() {
+    return (size_t)2 * NOPS * PL::SMW * 4 <= kSmemDoubleLimit ? NOPS * PL::SMW : 0;
+}
+template <class PL, int NOPS>
+__host__ __device__ constexpr size_t region_bytes() {
+    return (size_t)(region_stride<PL, NOPS>() ? 2 : 1) * NOPS * PL::SMW * 4;
+}
+
+// Per-prime constants a product kernel keeps in registers.
+struct PrimeCtx {
+    uint32_t p, pinv, r32, r32_sh, one_sh, qmodp;
+};
+
+__device__ __forceinline__ PrimeCtx load_prime_ctx(const BasisDev* __restrict__ B, int i) {
+    PrimeCtx c;
+    c.p = B->p[i];
+    c.pinv = B->pinv[i];
+    c.r32 = B->r32[i];
+    c.r32_sh = B->r32_sh[i];
+    c.one_sh = (uint32_t)(0x100000000ULL / c.p);  // Shoup companion of 1
+    c.qmodp = B->qmodp[i];
+    return c;
+}
+
+// 64-bit partial sum T (< 2^64) -> value in [0, 2p)
+__device__ __forceinline__ uint32_t fold64(uint64_t T, const PrimeCtx& c) {
+    const uint32_t hi = (uint32_t)(T >> 32), lo = (uint32_t)T;
+    const uint32_t a = shoup(hi, c.r32, c.r32_sh, c.p) + shoup(lo, 1u, c.one_sh, c.p);
+    return red(a, 2 * c.p);
+}
+
+// Residue of coefficient `pos` of a polynomial stored as [N][l64] limbs, in
+// [0, 4p) (valid forward-NTT input). `crt` (shared memory) holds 2^(32 j) mod p
+// for j < 2*l64 <= L32MAX. With CENTER, values above (q-1)/2 stand for x - q.
+template <bool CENTER>
+__device__ __forceinline__ uint32_t crt_coef(const uint64_t* __restrict__ src, int pos, int l64,
+                                             const uint32_t* crt, const uint32_t* qhalf, const PrimeCtx& c) {
+    const uint64_t* s = src + (size_t)pos * l64;
+    uint64_t T = 0;
+    uint32_t acc = 0;
+    bool gt = false;
+    for (int j = 0; j < l64; j++) {
+        const uint64_t limb = __ldg(s + j);
+        const uint32_t lo = (uint32_t)limb, hi = (uint32_t)(limb >> 32);
+        T += (uint64_t)lo * crt[2 * j] + (uint64_t)hi * crt[2 * j + 1];
+        if (CENTER) {
+            const uint32_t h0 = qhalf[2 * j], h1 = qhalf[2 * j + 1];
+            gt = (lo > h0) || (lo == h0 && gt);
+            gt = (hi > h1) || (hi == h1 && gt);
+        }
+        if ((j & 1) || j == l64 - 1) {  // at most 4 products of < 2^62 per partial sum
+            acc = red(acc + fold64(T, c), 2 * c.p);
+            T = 0;
+        }
+    }
+    if (CENTER && gt) acc = acc + 2 * c.p - c.qmodp;  // [0, 4p)
+    return acc;
+}
+
+// --------------------------------------------------------------------------
+// k_mul: one block per (prime, job); G = N/E threads
+// --------------------------------------------------------------------------
+template <int LOGN, int LOGE, bool CENTER>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+    k_mul(const BasisDev* __restrict__ B, const uint64_t* __restrict__ A, long long a_stride,
+          const uint64_t* __restrict__ Bv, long long b_stride, uint32_t* __restrict__ resid) {
+    using PL = NttPlan<LOGN, LOGE>;
+    constexpr int E = PL::E;
+    extern __shared__ uint32_t smem[];  // exchange regions, 2 operands x SMW each
+    __shared__ uint32_t s_crt[L32MAX];
+    __shared__ uint32_t s_qhalf[L32MAX];
+    const int tau = threadIdx.x;
+    const int prime = blockIdx.x;
+    const int job = blockIdx.y;
+    const int k = B->k, l64 = B->l64;
+    for (int i = tau; i < L32MAX; i += PL::G) {  // blocks of small N have fewer than L32MAX threads
+        s_crt[i] = B->crt[prime][i];
+        s_qhalf[i] = B->qhalf[i];
+    }
+    const PrimeCtx c = load_prime_ctx(B, prime);
+    const uint2* __restrict__ psi = B->psi[prime];
+    const uint2* __restrict__ ipsi = B->ipsi[prime];
+    __syncthreads();
+
+    const uint64_t* a = A + (size_t)job * a_stride;
+    const uint64_t* b = Bv + (size_t)job * b_stride;
+    uint32_t x[2][E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int pos = slot_pos<PL, 0>(tau, e);
+        x[0][e] = crt_coef<CENTER>(a, pos, l64, s_crt, s_qhalf, c);
+        x[1][e] = crt_coef<CENTER>(b, pos, l64, s_crt, s_qhalf, c);
+    }
+    constexpr int STRIDE = region_stride<PL, 2>();
+    int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0);
+    uint32_t z[1][E];
+#pragma unroll
+    for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
+    ntt_inverse<PL, 1>(z, ipsi, c.p, tau, smem, STRIDE, buf);
+    uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
+#pragma unroll
+    for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];
+}
+
+// --------------------------------------------------------------------------
+// k_keyswitch: one block per (prime, job). Digits are the 32-bit words of the
+// coefficients of c in [0, q) (w = 2^32), processed ND at a time.
+// evk: [ell][k][N] (value, Shoup companion) in the forward-NTT output order.
+// --------------------------------------------------------------------------
+template <int LOGN, int LOGE, int ND>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+    k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
+                int ell, uint32_t* __restrict__ resid) {
+    using PL = NttPlan<LOGN, LOGE>;
+    constexpr int E = PL::E;
+    constexpr int LAST = PL::NPASS - 1;
+    extern __shared__ uint32_t smem[];  // exchange regions, ND operands x SMW each
+    const int tau = threadIdx.x;
+    const int prime = blockIdx.x;
+    const int job = blockIdx.y;
+    const int k = B->k, l64 = B->l64;
+    const uint32_t p = B->p[prime];
+    const uint2* __restrict__ psi = B->psi[prime];
+    const uint2* __restrict__ ipsi = B->ipsi[prime];
+    const uint64_t* cj = C + (size_t)job * PL::N * l64;
+    constexpr int STRIDE = region_stride<PL, ND>();
+
+    uint32_t acc[1][E];
+#pragma unroll
+    for (int e = 0; e < E; e++) acc[0][e] = 0;
+    int buf = 0;
+    for (int d0 = 0; d0 < ell; d0 += ND) {
+        uint32_t x[ND][E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int pos = slot_pos<PL, 0>(tau, e);
+#pragma unroll
+            for (int o = 0; o < ND; o++) {
+                const int d = d0 + o;
+                uint32_t w = 0;
+                if (d < ell) {
+                    const uint64_t limb = __ldg(cj + (size_t)pos * l64 + (d >> 1));
+                    w = (uint32_t)(limb >> (32 * (d & 1)));
+                }
+                x[o][e] = red(w, 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
+            }
+        }
+        buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf);
+#pragma unroll
+        for (int o = 0; o < ND; o++) {
+            const int d = d0 + o;
+            if (d < ell) {
+                const uint2* __restrict__ g = evk + ((size_t)d * k + prime) * PL::N;
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const uint2 W = __ldg(g + slot_pos<PL, LAST>(tau, e));
+                    acc[0][e] = red(acc[0][e] + shoup(x[o][e], W.x, W.y, p), 2 * p);
+                }
+            }
+        }
+    }
+    ntt_inverse<PL, 1>(acc, ipsi, p, tau, smem, STRIDE, buf);
+    uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
+#pragma unroll
+    for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = acc[0][e];
+}
+
+// --------------------------------------------------------------------------
+// k_ntt: in-place transform of residue vectors [batch][k][N], values in [0, p).
+// Forward output in bit-reversed order; inverse includes N^-1.
+// --------------------------------------------------------------------------
+template <int LOGN, int LOGE, bool INV>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+    k_ntt(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv) {
+    using PL = NttPlan<LOGN, LOGE>;
+    constexpr int E = PL::E;
+    constexpr int LAST = PL::NPASS - 1;
+    extern __shared__ uint32_t smem[];
+    const int tau = threadIdx.x;
+    const int prime = blockIdx.x;
+    const int job = blockIdx.y;
+    const int k = B->k;
+    const uint32_t p = B->p[prime];
+    uint32_t* v = res + ((size_t)job * k + prime) * PL::N;
+    uint32_t x[1][E];
+    constexpr int STRIDE = region_stride<PL, 1>();
+    if (!INV) {
+#pragma unroll
+        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, 0>(tau, e)];
+        ntt_forward<PL, 1>(x, B->psi[prime], p, tau, smem, STRIDE, 0);
+#pragma unroll
+        for (int e = 0; e < E; e++) v[slot_pos<PL, LAST>(tau, e)] = red(red(x[0][e], 2 * p), p);
+    } else {
+        const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
+#pragma unroll
+        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
+        ntt_inverse<PL, 1>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0);
+#pragma unroll
+        for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
+    }
+}
+
+// --------------------------------------------------------------------------
+// k_epi: ICRT + mod q / round(t/q) / decrypt. One thread per coefficient.
+// L = 32-bit words of q.
+// --------------------------------------------------------------------------
+template <int L>
+struct Cols {
+    uint64_t c[L + 2];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int w = 0; w < L + 2; w++) c[w] = 0;
+    }
+    __device__ __forceinline__ void mac(uint32_t y, const uint32_t* a) {
+#pragma unroll
+        for (int w = 0; w < L; w++) c[w] += (uint64_t)y * a[w];
+    }
+    __device__ __forceinline__ void add(const uint32_t* a) {
+#pragma unroll
+        for (int w = 0; w < L; w++) c[w] += a[w];
+    }
+    // carry-propagate so that c[w] < 2^32 for w <= L
+    __device__ __forceinline__ void norm() {
+#pragma unroll
+        for (int w = 0; w < L + 1; w++) {
+            c[w + 1] += c[w] >> 32;
+            c[w] &= 0xFFFFFFFFULL;
+        }
+    }
+};
+
+// Barrett division of a normalised column value x (< 2^(32L+37)) by q' (top bit
+// of word L-1 set): returns the quotient, writes the remainder (< q') to r.
+template <int L>
+__device__ __forceinline__ uint64_t barrett(const Cols<L>& x, const uint32_t* qn, uint64_t mu, uint32_t (&r)[L]) {
+    const uint64_t x1 = (x.c[L + 1] << 33) | (x.c[L] << 1) | (x.c[L - 1] >> 31);  // floor(x / 2^(32L-1)) < 2^38
+    const uint64_t hi = __umul64hi(x1, mu), lo = x1 * mu;
+    uint64_t Q = (hi << 26) | (lo >> 38);  // Q-2 <= Q <= Q_true
+    const uint32_t Ql = (uint32_t)Q, Qh = (uint32_t)(Q >> 32);
+    uint32_t P[L + 2];
+    uint64_t carry = 0;
+#pragma unroll
+    for (int w = 0; w < L; w++) {
+        const uint64_t t = (uint64_t)Ql * qn[w] + carry;
+        P[w] = (uint32_t)t;
+        carry = t >> 32;
+    }
+    P[L] = (uint32_t)carry;
+    carry = 0;
+#pragma unroll
+    for (int w = 0; w < L; w++) {
+        const uint64_t t = (uint64_t)Qh * qn[w] + P[w + 1] + carry;
+        P[w + 1] = (uint32_t)t;
+        carry = t >> 32;
+    }
+    P[L + 1] = (uint32_t)carry;
+    uint32_t rr[L + 1];
+    int64_t br = 0;
+#pragma unroll
+    for (int w = 0; w <= L; w++) {
+        const int64_t d = (int64_t)x.c[w] - (int64_t)P[w] - br;
+        rr[w] = (uint32_t)d;
+        br = d < 0;
+    }
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        uint32_t t[L + 1];
+        int64_t b2 = 0;
+#pragma unroll
+        for (int w = 0; w < L; w++) {
+            const int64_t d = (int64_t)rr[w] - (int64_t)qn[w] - b2;
+            t[w] = (uint32_t)d;
+            b2 = d < 0;
+        }
+        const int64_t d = (int64_t)rr[L] - b2;
+        t[L] = (uint32_t)d;
+        b2 = d < 0;
+        if (!b2) {
+#pragma unroll
+            for (int w = 0; w <= L; w++) rr[w] = t[w];
+            Q++;
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < L; w++) r[w] = rr[w];
+    return Q;
+}
+
+struct EpiShared {
+    uint32_t p[KMAX], ycon[KMAX], ycon_sh[KMAX], flo[KMAX], fhi[KMAX];
+    uint32_t A0[KMAX * L32MAX];
+    uint32_t A1[KMAX * L32MAX];
+    uint32_t B0[L32MAX], B1[L32MAX], qn[L32MAX], qhalf_n[L32MAX];
+};
+
+template <int L, int MODE>
+__global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
+                                             void* __restrict__ out, int njobs) {
+    __shared__ EpiShared S;
+    const int k = B->k, logn = B->logn, shift = B->shift, l64 = B->l64;
+    const uint64_t mu = B->mu;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        S.p[i] = B->p[i];
+        S.ycon[i] = B->ycon[i];
+        S.ycon_sh[i] = B->ycon_sh[i];
+        S.flo[i] = B->flo[i];
+        S.fhi[i] = B->fhi[i];
+    }
+    for (int i = threadIdx.x; i < k * L; i += blockDim.x) {
+        S.A0[i] = B->A0[i / L][i % L];
+        if (MODE == EPI_YASHE) S.A1[i] = B->A1[i / L][i % L];
+    }
+    if (threadIdx.x < L) {
+        S.B0[threadIdx.x] = B->B0[threadIdx.x];
+        S.B1[threadIdx.x] = B->B1[threadIdx.x];
+        S.qn[threadIdx.x] = B->qn[threadIdx.x];
+        S.qhalf_n[threadIdx.x] = B->qhalf_n[threadIdx.x];
+    }
+    __syncthreads();
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = 1 << logn;
+    const long long job = idx >> logn;
+    if (job >= njobs) return;
+    const int coef = (int)(idx & (n - 1));
+    const uint32_t* r0 = resid + (size_t)job * k * n + coef;
+
+    Cols<L> c0, c1;
+    c0.zero();
+    c1.zero();
+    uint64_t vacc = 0;
+    int pending = 0;
+    for (int i = 0; i < k; i++) {
+        const uint32_t r = __ldcg(r0 + (size_t)i * n);
+        const uint32_t p = S.p[i];
+        const uint32_t y = red(shoup(r, S.ycon[i], S.ycon_sh[i], p), p);  // [X Mhat_i^-1]_{p_i}
+        vacc += (uint64_t)y * S.fhi[i] + __umulhi(y, S.flo[i]);          // sum y_i/p_i in 2^-32 units
+        c0.mac(y, &S.A0[i * L]);
+        if (MODE == EPI_YASHE) c1.mac(y, &S.A1[i * L]);
+        if (++pending == 3) {
+            c0.norm();
+            if (MODE == EPI_YASHE) c1.norm();
+            pending = 0;
+        }
+    }
+    const uint32_t v = (uint32_t)((vacc + 0x80000000ULL) >> 32);  // round(sum y_i/p_i): X = sum y_i Mhat_i - v M
+    c0.norm();
+    c0.mac(v, S.B0);
+    if (MODE == EPI_YASHE) {
+        c1.norm();
+        c1.mac(v, S.B1);
+        c1.add(S.qhalf_n);
+        c1.norm();
+        uint32_t rdummy[L];
+        const uint64_t Q2 = barrett<L>(c1, S.qn, mu, rdummy);  // round(S/q) + v, S = sum y_i R_i - v R_M
+        // c0 += Q2 << shift
+        const uint64_t lo = Q2 << shift;
+        const uint64_t hi = shift ? (Q2 >> (64 - shift)) : 0;
+        c0.c[0] += (uint32_t)lo;
+        c0.c[1] += (uint32_t)(lo >> 32);
+        c0.c[2] += hi;
+    }
+    c0.norm();
+    uint32_t r[L];
+    barrett<L>(c0, S.qn, mu, r);  // r = (result mod q) << shift
+    if constexpr (MODE == EPI_DECRYPT) {
+        Cols<L> c2;
+        c2.zero();
+        c2.mac(B->t, r);
+        c2.add(S.qhalf_n);
+        c2.norm();
+        uint32_t rd[L];
+        uint64_t Q = barrett<L>(c2, S.qn, mu, rd);  // round(t x / q) in [0, t]
+        if (Q >= B->t) Q -= B->t;
+        reinterpret_cast<uint64_t*>(out)[job * n + coef] = Q;
+    } else {
+        uint32_t o[L];
+#pragma unroll
+        for (int w = 0; w < L; w++) {
+            const uint32_t nx = (w + 1 < L) ? r[w + 1] : 0u;
+            o[w] = __funnelshift_r(r[w], nx, shift);
+        }
+        uint64_t* dst = reinterpret_cast<uint64_t*>(out) + ((size_t)job * n + coef) * l64;
+#pragma unroll
+        for (int j = 0; j < (L + 1) / 2; j++) {
+            const uint64_t lo32 = o[2 * j];
+            const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
+            dst[j] = lo32 | (hi32 << 32);
+        }
+    }
+}
+
+}  // namespace cy
+
+namespace cy {
+
+template <int LOGN, int LOGE>
+void fill_kernel_set(KernelSet& ks) {
+    using PL = NttPlan<LOGN, LOGE>;
+    ks.logn = LOGN;
+    ks.loge = LOGE;
+    ks.threads = PL::G;
+    ks.mul[0] = (void*)k_mul<LOGN, LOGE, false>;
+    ks.mul[1] = (void*)k_mul<LOGN, LOGE, true>;
+    ks.ks[0] = (void*)k_keyswitch<LOGN, LOGE, 2>;
+    ks.ks[1] = (void*)k_keyswitch<LOGN, LOGE, 4>;
+    ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
+    ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
+    ks.smem_mul = region_bytes<PL, 2>();
+    ks.smem_ks[0] = region_bytes<PL, 2>();
+    ks.smem_ks[1] = region_bytes<PL, 4>();
+    ks.smem_ntt = region_bytes<PL, 1>();
+}
+
+}  // namespace cy

@@ -1,0 +1,206 @@
+// ntt_core.cuh -- negacyclic NTT of length N = 2^LOGN held in registers.
+//
+// The reference runs one radix-2 Stockham stage per kernel launch, through
+// global memory, with one block per residue (NTT / NTTIteration,
+// src/cuda_functions.cu:404-458; 3*log2(n) launches per product). Here a thread
+// block of G = N/E threads owns one length-N transform: every thread keeps E
+// coefficients in registers, the log2(N) stages are grouped into passes of at
+// most LOGE stages that run entirely in registers, and consecutive passes swap
+// data through a padded shared-memory buffer (one barrier per swap, two
+// alternating buffers). Several operands (NOPS) of the same prime share the
+// twiddle loads and interleave for instruction-level parallelism.
+//
+// Transform (merged negacyclic twist): forward Cooley-Tukey on natural-order
+// input with twiddles psi^bitrev(m+i), output in bit-reversed order; inverse
+// Gentleman-Sande on bit-reversed input with psi^-bitrev(m+i), natural-order
+// output, without the N^-1 factor (folded into the ICRT constants). So
+// INTT(NTT(a) . NTT(b)) = N * a*b mod (x^N + 1, p): the fold by x^N + 1 that the
+// reference does on the host (src/cuda_functions.cu:1061-1072) is implicit.
+//
+// Index map of a pass that covers stages s0 .. s0+R-1 (stage s pairs j and
+// j + N/2^(s+1)): with d = N >> (s0 + R), a butterfly group is the 2^R
+// positions g*2^R*d + r + u*d (u < 2^R); thread tau owns groups
+// gamma = tau + v*G (v < E/2^R) with g = gamma / d, r = gamma % d. The
+// twiddle of stage s0+l for element u is tw[2^(s0+l) + g*2^l + (u >> (R-l))].
+#pragma once
+
+#include <stdint.h>
+
+#include "arith.cuh"
+
+namespace cy {
+
+template <int LOGN_, int LOGE_>
+struct NttPlan {
+    static constexpr int LOGN = LOGN_;
+    static constexpr int LOGE = LOGE_;
+    static constexpr int N = 1 << LOGN;
+    static constexpr int E = 1 << LOGE;
+    static constexpr int G = N >> LOGE;  // threads per transform
+    static constexpr int NPASS = (LOGN + LOGE - 1) / LOGE;
+    static constexpr int R0 = LOGN - (NPASS - 1) * LOGE;  // the first pass takes the remainder
+    static constexpr int SMW = N + (N >> 5);               // padded words per operand buffer
+    __host__ __device__ static constexpr int R(int pass) { return pass == 0 ? R0 : LOGE; }
+    __host__ __device__ static constexpr int S0(int pass) { return pass == 0 ? 0 : R0 + (pass - 1) * LOGE; }
+    __host__ __device__ static constexpr int LOGD(int pass) { return LOGN - S0(pass) - R(pass); }
+};
+
+// one padding word per 32: position -> shared-memory word
+__device__ __forceinline__ int padi(int pos) { return pos + (pos >> 5); }
+__host__ __device__ constexpr int padc(int c) { return c + (c >> 5); }
+
+// position of the first element of group v of thread tau in pass PASS
+template <class PL, int PASS>
+__device__ __forceinline__ int group_base(int tau, int v) {
+    constexpr int R = PL::R(PASS), LOGD = PL::LOGD(PASS);
+    const int gam = tau + (v << (PL::LOGN - PL::LOGE));
+    const int g = gam >> LOGD;
+    const int r = gam & ((1 << LOGD) - 1);
+    return (g << (LOGD + R)) | r;
+}
+
+// position of slot e (= v*2^R + u) of thread tau in pass PASS
+template <class PL, int PASS>
+__device__ __forceinline__ int slot_pos(int tau, int e) {
+    constexpr int R = PL::R(PASS), LOGD = PL::LOGD(PASS);
+    return group_base<PL, PASS>(tau, e >> R) + ((e & ((1 << R) - 1)) << LOGD);
+}
+
+template <class PL, int PASS, int NOPS>
+__device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+                                         int tau) {
+    constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
+    constexpr int GS = 1 << R;
+    constexpr int NV = PL::E >> R;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        const int gam = tau + (v << (PL::LOGN - PL::LOGE));
+        const int g = (S0 == 0) ? 0 : (gam >> LOGD);
+#pragma unroll
+        for (int l = 0; l < R; l++) {
+            const int half = 1 << (R - 1 - l);
+            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);
+#pragma unroll
+            for (int h = 0; h < (1 << l); h++) {
+                const uint2 W = __ldg(twl + h);
+#pragma unroll
+                for (int j = 0; j < half; j++) {
+                    const int u = (h << (R - l)) + j;
+#pragma unroll
+                    for (int o = 0; o < NOPS; o++) ct_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
+                }
+            }
+        }
+    }
+}
+
+template <class PL, int PASS, int NOPS>
+__device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+                                         int tau) {
+    constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
+    constexpr int GS = 1 << R;
+    constexpr int NV = PL::E >> R;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        const int gam = tau + (v << (PL::LOGN - PL::LOGE));
+        const int g = (S0 == 0) ? 0 : (gam >> LOGD);
+#pragma unroll
+        for (int l = R - 1; l >= 0; l--) {
+            const int half = 1 << (R - 1 - l);
+            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);
+#pragma unroll
+            for (int h = 0; h < (1 << l); h++) {
+                const uint2 W = __ldg(twl + h);
+#pragma unroll
+                for (int j = 0; j < half; j++) {
+                    const int u = (h << (R - l)) + j;
+#pragma unroll
+                    for (int o = 0; o < NOPS; o++) gs_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
+                }
+            }
+        }
+    }
+}
+
+// Registers laid out for pass PA -> registers laid out for pass PB, through
+// shared memory `sm` (NOPS buffers of SMW words). Callers that alternate
+// between two such regions need one barrier (the next write cannot race with a
+// slow reader of this region); a caller with a single region passes
+// `sync_before` to add a barrier ahead of the writes.
+template <class PL, int PA, int PB, int NOPS>
+__device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* sm, int tau, bool sync_before) {
+    constexpr int RA = PL::R(PA), LA = PL::LOGD(PA), NVA = PL::E >> RA;
+    constexpr int RB = PL::R(PB), LB = PL::LOGD(PB), NVB = PL::E >> RB;
+    if (sync_before) __syncthreads();
+#pragma unroll
+    for (int v = 0; v < NVA; v++) {
+        const int base = padi(group_base<PL, PA>(tau, v));
+#pragma unroll
+        for (int u = 0; u < (1 << RA); u++) {
+#pragma unroll
+            for (int o = 0; o < NOPS; o++) sm[o * PL::SMW + base + padc(u << LA)] = x[o][(v << RA) + u];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < NVB; v++) {
+        const int base = padi(group_base<PL, PB>(tau, v));
+#pragma unroll
+        for (int u = 0; u < (1 << RB); u++) {
+#pragma unroll
+            for (int o = 0; o < NOPS; o++) x[o][(v << RB) + u] = sm[o * PL::SMW + base + padc(u << LB)];
+        }
+    }
+}
+
+// Forward passes PASS .. NPASS-1. `buf` counts the exchanges made so far by the
+// block; exchange number b uses region (b & 1) of `sm`, regions `stride` words
+// apart (stride >= NOPS * SMW for every NOPS the kernel uses), or the single
+// region `sm` when stride == 0. Returns the updated count.
+template <class PL, int PASS, int NOPS>
+struct FwdFrom {
+    __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
+                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf) {
+        if constexpr (PASS >= PL::NPASS) {
+            return buf;
+        } else {
+            exchange<PL, PASS - 1, PASS, NOPS>(x, sm + (buf & 1) * stride, tau, stride == 0);
+            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau);
+            return FwdFrom<PL, PASS + 1, NOPS>::run(x, tw, p, tau, sm, stride, buf + 1);
+        }
+    }
+};
+
+// Inverse passes PASS .. 0 where pass PASS+1 was the previous one.
+template <class PL, int PASS, int NOPS>
+struct InvFrom {
+    __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
+                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf) {
+        if constexpr (PASS < 0) {
+            return buf;
+        } else {
+            exchange<PL, PASS + 1, PASS, NOPS>(x, sm + (buf & 1) * stride, tau, stride == 0);
+            inv_pass<PL, PASS, NOPS>(x, tw, p, tau);
+            return InvFrom<PL, PASS - 1, NOPS>::run(x, tw, p, tau, sm, stride, buf + 1);
+        }
+    }
+};
+
+// Full forward transform: registers in pass-0 layout (natural order) ->
+// registers in last-pass layout (bit-reversed order).
+template <class PL, int NOPS>
+__device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+                                           int tau, uint32_t* sm, int stride, int buf) {
+    fwd_pass<PL, 0, NOPS>(x, tw, p, tau);
+    return FwdFrom<PL, 1, NOPS>::run(x, tw, p, tau, sm, stride, buf);
+}
+
+// Full inverse transform: registers in last-pass layout -> pass-0 layout.
+template <class PL, int NOPS>
+__device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+                                           int tau, uint32_t* sm, int stride, int buf) {
+    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau);
+    return InvFrom<PL, PL::NPASS - 2, NOPS>::run(x, tw, p, tau, sm, stride, buf);
+}
+
+}  // namespace cy

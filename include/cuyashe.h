@@ -1,0 +1,217 @@
+/*
+ * cuyashe.h -- C ABI of the GB300-native (sm_103a) cuYASHE hot path.
+ *
+ * The reference crosses from host C++ into CUDA only through the static
+ * launchers of `class CUDAFunctions` (src/cuda_functions.h:19-84) and the free
+ * functions callCRT / callICRT / callCuModN (src/cuda_bn.h:76-87). Above them sit
+ * `Polynomial` (src/polynomial.h), `Ciphertext` (src/ciphertext.h) and `Yashe`
+ * (src/yashe.h). This header replaces that boundary with plain C: opaque
+ * handles, caller-owned buffers, explicit streams, status codes.
+ *
+ * Data layout. A polynomial of a ring with N coefficients and modulus q is N
+ * coefficients of L = ceil(bits(q)/64) little-endian uint64 limbs each
+ * ([N][L]); a batch is [batch][N][L]. Inputs must lie in [0, q). The `d_`
+ * prefix marks device pointers, `h_` host pointers.
+ *
+ * Errors. Every function returns a cy_status; none aborts or throws. The
+ * reference asserts on every CUDA result and throws `const char*`
+ * (src/polynomial.cpp:424,450; src/cuda_bn.cu:1145). cy_last_error() returns a
+ * per-thread message for the last failure.
+ *
+ * Threading. A handle may be used from several threads as long as calls that
+ * share a handle's internal workspace do not overlap on the GPU: calls on one
+ * handle are ordered on the stream they are given; calls on different streams
+ * need their own cy_workspace (cy_*_ws variants). The reference keeps all state
+ * in process-wide statics (src/polynomial.h:35-41, src/cuda_functions.cu:23-38)
+ * and always uses stream 0 (src/polynomial.h:1384-1387).
+ */
+#ifndef CUYASHE_GB300_H
+#define CUYASHE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cy_status {
+    CY_OK = 0,
+    CY_ERR_INVALID_ARGUMENT = -1,
+    CY_ERR_UNSUPPORTED = -2,
+    CY_ERR_CUDA = -3,
+    CY_ERR_OUT_OF_MEMORY = -4,
+    CY_ERR_NOT_INVERTIBLE = -5,
+    CY_ERR_NO_KEYS = -6,
+    CY_ERR_TIMEOUT = -7,
+    CY_ERR_BUSY = -8,
+    CY_ERR_INTERNAL = -9
+} cy_status;
+
+/* A cudaStream_t; NULL means the legacy default stream. */
+typedef void *cy_stream_t;
+
+/* Limits of this build. */
+#define CY_MAX_LOGN 14        /* N up to 16384 */
+#define CY_MAX_Q_BITS 384     /* q up to 384 bits (6 limbs) */
+#define CY_MAX_CRT_PRIMES 40  /* word-sized NTT primes per basis */
+
+const char *cy_status_string(int status);
+const char *cy_last_error(void);
+int cy_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Rings Z_q[x]/(x^N+1)                                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct cy_ring cy_ring;
+typedef struct cy_workspace cy_workspace;
+
+typedef struct cy_ring_info {
+    int n;              /* coefficients */
+    int q_limbs;        /* 64-bit limbs per coefficient */
+    int q_bits;
+    int crt_primes;     /* primes of the product basis */
+    int crt_bits;       /* bits of their product M */
+    uint32_t primes[CY_MAX_CRT_PRIMES];
+} cy_ring_info;
+
+/* Builds the ring for N (power of two, 2..16384) and q < 2^384: picks the
+ * word-sized NTT-friendly CRT basis with M > 4*N*q^2 (the reference's rule,
+ * src/polynomial.h:914, is M >= 2*N*q^2), uploads twiddles and CRT/ICRT
+ * constants. Replaces Polynomial::gen_crt_primes (src/polynomial.h:898-955),
+ * CUDAFunctions::write_crt_primes (src/cuda_bn.cu:1047-1146) and
+ * CUDAFunctions::init (src/cuda_functions.cu:878-956). The ring is bound to the
+ * CUDA device current at creation. */
+cy_status cy_ring_create(int n, const uint64_t *h_q, int q_limbs, cy_ring **out);
+cy_status cy_ring_destroy(cy_ring *ring);
+cy_status cy_ring_get_info(const cy_ring *ring, cy_ring_info *info);
+
+/* Scratch for calls that run on different streams at the same time. A NULL
+ * workspace means the ring's own (grown on demand with cudaMalloc). */
+cy_status cy_workspace_create(cy_workspace **out);
+cy_status cy_workspace_destroy(cy_workspace *ws);
+
+/* c = a*b mod (x^N+1, q) for `batch` independent products.
+ * Replaces `Polynomial c = a*b; c.reduce();` (src/polynomial.cpp:52-60,
+ * src/common.h:136-226, src/cuda_functions.cu:617-738 and :1040-1077):
+ * CRT split, forward NTTs, pointwise product, inverse NTT, ICRT and mod q all
+ * run on the GPU. Asynchronous on `stream`. */
+cy_status cy_polymul(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
+                     cy_stream_t stream);
+cy_status cy_polymul_ws(cy_ring *ring, cy_workspace *ws, const uint64_t *d_a, const uint64_t *d_b,
+                        uint64_t *d_c, int batch, cy_stream_t stream);
+
+/* Same product with host buffers: copies in, multiplies, copies out, and
+ * synchronises (the reference's with-memcopy path, src/benchmark_polynomial.cpp:361-388). */
+cy_status cy_polymul_host(cy_ring *ring, const uint64_t *h_a, const uint64_t *h_b, uint64_t *h_c, int batch);
+
+/* c = a + b mod q and c = a - b mod q, elementwise over the batch.
+ * Replaces callPolynomialAddSub (src/cuda_functions.cu:99-165), which adds
+ * residues without reduction. */
+cy_status cy_polyadd(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
+                     cy_stream_t stream);
+cy_status cy_polysub(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
+                     cy_stream_t stream);
+
+/* c = s*a mod q for a scalar s in [0, q) given as q_limbs limbs.
+ * Replaces Polynomial::operator*(ZZ) / callPolynomialOPInteger (MUL)
+ * (src/polynomial.h:533-573, src/cuda_functions.cu:477-547). */
+cy_status cy_poly_scalar_mul(cy_ring *ring, const uint64_t *d_a, const uint64_t *h_scalar, uint64_t *d_c,
+                             int batch, cy_stream_t stream);
+
+/* Mixed batch: products of different rings (different N and q) in one
+ * submission. Jobs are grouped by ring and launched back to back on `stream`. */
+typedef struct cy_polymul_job {
+    cy_ring *ring;
+    const uint64_t *d_a;
+    const uint64_t *d_b;
+    uint64_t *d_c;
+} cy_polymul_job;
+cy_status cy_polymul_batched(const cy_polymul_job *jobs, int njobs, cy_stream_t stream);
+
+/* Forward / inverse negacyclic NTT of residue vectors: d_res is [batch][k][N]
+ * uint32 residues modulo the ring's CRT primes, transformed in place (values
+ * in [0, p) on input and output; forward output in bit-reversed order, inverse
+ * output scaled by N^-1). Replaces CUDAFunctions::callNTT
+ * (src/cuda_functions.cu:447-458). */
+cy_status cy_ntt(cy_ring *ring, uint32_t *d_res, int batch, int inverse, cy_stream_t stream);
+
+/* CRT split and ICRT recombination on their own (callCRT / callICRT,
+ * src/cuda_bn.cu:970-1045): d_res [batch][k][N] uint32 <-> d_x [batch][N][L]. */
+cy_status cy_crt(cy_ring *ring, const uint64_t *d_x, uint32_t *d_res, int batch, cy_stream_t stream);
+cy_status cy_icrt(cy_ring *ring, const uint32_t *d_res, uint64_t *d_x, int batch, cy_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* YASHE (Bos, Lauter, Loftus, Naehrig 2013)                                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct cy_yashe cy_yashe;
+
+typedef struct cy_yashe_params {
+    int n;               /* ring degree N */
+    const uint64_t *q;   /* ciphertext modulus, q_limbs limbs, odd */
+    int q_limbs;
+    uint64_t t;          /* plaintext modulus, 2 <= t < 2^32 */
+    int w_bits;          /* relinearisation digit width; 32 */
+    double sigma;        /* error parameter of the discrete Gaussian (8.0) */
+} cy_yashe_params;
+
+typedef struct cy_yashe_info {
+    int n, q_limbs, q_bits, ell, w_bits;
+    uint64_t t;
+    int tensor_primes;   /* CRT basis of the tensor product */
+    int relin_primes;    /* CRT basis of the keyswitch */
+    int has_keys;
+} cy_yashe_info;
+
+/* Replaces the statics Yashe::{d,q,t,w,lwq} (src/yashe.h:17-29) and their set-up
+ * in the reference's fixtures (src/test.cu:73-133). */
+cy_status cy_yashe_create(const cy_yashe_params *params, cy_yashe **out);
+cy_status cy_yashe_destroy(cy_yashe *y);
+cy_status cy_yashe_get_info(const cy_yashe *y, cy_yashe_info *info);
+cy_status cy_yashe_get_ring(cy_yashe *y, cy_ring **ring);
+
+/* Key generation on the host (set-up time): f = t*f'+1 with ternary f', real
+ * f^-1 in R_q, h = [t*g*f^-1]_q, evk_d = [f*w^d + e_d + h*s_d]_q. The evaluation
+ * key is then kept resident on the GPU in the NTT domain. Replaces
+ * Yashe::generate_keys (src/yashe.cpp:17-102), which stubs f^-1 with f. */
+cy_status cy_yashe_keygen(cy_yashe *y, uint64_t seed);
+
+/* Installs externally generated keys (host arrays): f [N][L], h [N][L],
+ * evk [ell][N][L]. */
+cy_status cy_yashe_set_keys(cy_yashe *y, const uint64_t *h_f, const uint64_t *h_h, const uint64_t *h_evk);
+cy_status cy_yashe_get_keys(const cy_yashe *y, uint64_t *h_f, uint64_t *h_h, uint64_t *h_evk);
+
+/* c = [Delta*m + e + h*s]_q on the host (set-up time); m: [batch][N] uint64 in
+ * [0, t); ct: [batch][N][L]. Replaces Yashe::encrypt (src/yashe.cpp:104-142). */
+cy_status cy_yashe_encrypt_host(cy_yashe *y, const uint64_t *h_m, uint64_t *h_ct, int batch, uint64_t seed);
+
+/* m = [round(t/q * [key*c]_q)]_t on the GPU for every coefficient; key = f, or
+ * f^2 when `aftermul` (a product that was not relinearised). m: [batch][N]
+ * uint64. Replaces Yashe::decrypt (src/yashe.cpp:143-201), which decrypts
+ * coefficient 0 only. */
+cy_status cy_yashe_decrypt(cy_yashe *y, const uint64_t *d_ct, uint64_t *d_m, int batch, int aftermul,
+                           cy_stream_t stream);
+
+/* Homomorphic multiply: out = [round(t/q * c1*c2)]_q with the product over
+ * Z[x]/(x^N+1) on symmetric representatives, then (relin != 0) the keyswitch
+ * [sum_d D_d(out)*evk_d]_q. Replaces Ciphertext::operator* and
+ * Ciphertext::convert/keyswitch (src/ciphertext.cpp:38-130). */
+cy_status cy_yashe_mul(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out, int batch,
+                       int relin, cy_stream_t stream);
+cy_status cy_yashe_mul_ws(cy_yashe *y, cy_workspace *ws, const uint64_t *d_c1, const uint64_t *d_c2,
+                          uint64_t *d_out, int batch, int relin, cy_stream_t stream);
+
+/* Relinearisation alone: out = [sum_d D_d(c)*evk_d]_q (Ciphertext::convert). */
+cy_status cy_yashe_keyswitch(cy_yashe *y, const uint64_t *d_c, uint64_t *d_out, int batch, cy_stream_t stream);
+
+/* Homomorphic add (Ciphertext::operator+, src/ciphertext.cpp:4-23). */
+cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out, int batch,
+                       cy_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUYASHE_GB300_H */
