@@ -1,0 +1,424 @@
+#!/usr/bin/env python3
+"""Benchmark of the cuYASHE hot path on GB300.
+
+Workload (one step): one batched YASHE homomorphic multiply with
+relinearisation, N = 4096, q = a 127-bit prime (q = 1 mod 2^16), t = 1024,
+w = 2^32 (4 digits), over B ciphertext pairs resident in HBM
+(cy_yashe_mul, relin = 1). Reported beside it, outside the headline:
+  * the plain per-call path (one HE multiply per call, synchronised),
+  * batched and per-call polynomial products at N = 4096, q = 2^127 - 1,
+  * e2e: the same multiply through host buffers with the copies timed,
+  * per-kernel device times (CUDA events) and the roofline of the top kernel,
+  * the reference's CPU multiply (C restatement) timed on the host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "polymul/s & HE mults/s at N=4096, batched vs plain, bit-exact; % HBM roofline"
+N = 4096
+Q_YASHE = 170141183460469231731687303715883253761  # largest prime < 2^127 with q = 1 (mod 2^16)
+Q_POLY = 2**127 - 1                                 # the reference benchmark's q
+T = 1024
+W_BITS = 32
+L = 2                                               # uint64 limbs per coefficient
+CT_BYTES = N * L * 8                                # one ciphertext / polynomial
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# reference arm / CPU baseline: the oracle's C restatement of the reference
+# ----------------------------------------------------------------------------
+
+def cpu_yashe_rate(pairs: int, threads: int, c1, c2, evk):
+    """HE mults/s of the reference's multiply (restated in C) on `pairs` pairs."""
+    from oracle import refpath
+
+    rp = refpath.RefPath(Q_YASHE, N)
+    t0 = time.perf_counter()
+    rp.yashe_mul(c1[:pairs], c2[:pairs], T, W_BITS, evk, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return pairs / dt, dt
+
+
+def synthetic_host_cts(pairs: int, seed: int):
+    """Ciphertext-shaped inputs uniform in [0, 2^126) (below q; fresh YASHE
+    ciphertexts are computationally indistinguishable from uniform) and an
+    evaluation key of the same shape (4 digits)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+
+    def uni(shape):
+        lo = rng.integers(0, 2**64, size=shape, dtype=np.uint64)
+        hi = rng.integers(0, 2**62, size=shape, dtype=np.uint64)
+        return np.ascontiguousarray(np.stack([lo, hi], axis=-1))
+    return uni((pairs, N)), uni((pairs, N)), uni((4, N))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    c1, c2, evk = synthetic_host_cts(max(threads, 8), 1)
+    pairs = max(threads, 8)
+    rates = []
+    for _ in range(args.warmup):
+        cpu_yashe_rate(min(pairs, threads), threads, c1, c2, evk)
+    for _ in range(args.steps):
+        r, _ = cpu_yashe_rate(pairs, threads, c1, c2, evk)
+        rates.append(r)
+    v = statistics.median(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "HE mults/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * pairs / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 (reference CPU multiply, C restatement)",
+                   "pairs_per_step": pairs, "host_threads": threads},
+        "cpu_baseline": {"value": v, "unit": "HE mults/s", "cores": threads, "kind": "port",
+                         "sample": "%d HE multiplies per step at N=4096 (29-bit CRT bucket, Goldilocks Stockham NTT)"
+                                   % pairs},
+        "e2e": {"value": v, "unit": "HE mults/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+
+def make_inputs(Y, batch: int, pool: int, seed: int):
+    """Fresh encryptions (library keygen + encryption), tiled to `batch` pairs."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(seed)
+    m1 = rng.integers(0, T, size=(pool, N), dtype=np.uint64)
+    m2 = rng.integers(0, T, size=(pool, N), dtype=np.uint64)
+    ct1 = Y.encrypt_host(m1, seed=seed + 1)
+    ct2 = Y.encrypt_host(m2, seed=seed + 2)
+    idx1 = np.arange(batch) % pool
+    idx2 = (np.arange(batch) * 7 + 3) % pool
+    C1 = torch.from_numpy(ct1.view(np.int64)).cuda()[torch.from_numpy(idx1).cuda()].contiguous()
+    C2 = torch.from_numpy(ct2.view(np.int64)).cuda()[torch.from_numpy(idx2).cuda()].contiguous()
+    return C1, C2, m1, m2, idx1, idx2
+
+
+def time_steps(fn, steps: int, stream):
+    import torch
+
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    end.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end)
+
+
+def kernel_bytes(name: str, launches: int, jobs: int, k_tensor: int, k_relin: int, ell: int):
+    """Algorithmic bytes moved by all launches of one kernel over `jobs` jobs."""
+    res = N * 4
+    if name.startswith("mul_centered"):
+        return jobs * (2 * CT_BYTES + k_tensor * res)
+    if name.startswith("keyswitch"):
+        return jobs * (CT_BYTES + k_relin * res) + launches * ell * k_relin * N * 8
+    if name.startswith("epi_yashe"):
+        return jobs * (k_tensor * res + CT_BYTES)
+    if name.startswith("epi_modq"):
+        return jobs * (k_relin * res + CT_BYTES)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import cuyashe_gb300 as cy
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    cy.lib()
+    stream = torch.cuda.current_stream()
+    B = args.batch
+
+    # ---- set-up (untimed): keys, fresh encryptions, correctness check --------
+    Y = cy.Yashe(N, Q_YASHE, T, W_BITS, 8.0)
+    Y.keygen(1234 + rank)
+    C1, C2, m1, m2, idx1, idx2 = make_inputs(Y, B, pool=32, seed=77 + rank)
+    OUT = Y.ring.empty(B)
+    Y.mul(C1, C2, relin=True, out=OUT)
+    dec = Y.decrypt(OUT[:4]).cpu().numpy().view(np.uint64)
+    PT = cy.Ring(N, T)  # plaintext ring Z_t[x]/(x^N+1): reference products on the GPU
+    exp = PT.polymul(PT.upload(m1[idx1[:4]].astype(object).tolist()),
+                     PT.upload(m2[idx2[:4]].astype(object).tolist()))
+    exp = exp.cpu().numpy().view(np.uint64)[..., 0]
+    torch.cuda.synchronize()
+    decrypt_ok = bool((dec == exp).all())
+    log("decrypt(c1*c2) == m1*m2 mod t:", decrypt_ok)
+
+    def step():
+        Y.mul(C1, C2, relin=True, out=OUT)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if args.ncu_step:
+        # one step between cudaProfilerStart/Stop for `ncu --profile-from-start off`
+        torch.cuda.profiler.start()
+        step()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        log("ncu step done")
+        return
+
+    # ---- timed region -----------------------------------------------------------
+    launches0 = cy.launch_count()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clocks:
+        ms = time_steps(step, args.steps, stream)
+    launches = cy.launch_count() - launches0
+    ms_t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = world * B * args.steps / (ms_max / 1000.0)
+    log("batched HE mults/s: %.1f (%.3f ms/step, batch %d)" % (value, ms_max / args.steps, B))
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # ---- per-kernel device times (one traced step, outside the timed region) ----
+    info = Y.info()
+    with cy.Trace() as tr:
+        step()
+    kernels = {}
+    for name, (cnt, kms) in tr.kernels.items():
+        kernels[name] = {"launches": cnt, "ms": round(kms, 4)}
+    total_k = sum(v["ms"] for v in kernels.values()) or 1.0
+    for v in kernels.values():
+        v["share"] = round(v["ms"] / total_k, 4)
+    top = max(kernels, key=lambda k: kernels[k]["ms"])
+    peak, peak_kind = read_peaks()
+    top_bytes = kernel_bytes(top, kernels[top]["launches"], B, info.tensor_primes, info.relin_primes, info.ell)
+    top_gbs = top_bytes / (kernels[top]["ms"] / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_job.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        per_job = tj.get(top.split("_n")[0])
+        if per_job:
+            traffic = per_job * B / kernels[top]["launches"]
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(top_gbs, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(top_gbs / peak, 4), "peak_kind": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": top_bytes / kernels[top]["launches"]}
+    step_bytes = B * 3 * CT_BYTES + info.ell * N * L * 8
+    step_gbs = step_bytes / (ms_max / args.steps / 1000.0) / 1e9
+
+    # ---- plain per-call path: one HE multiply per call, synchronised ------------
+    plain_calls = 200
+    o1 = Y.ring.empty(1)
+
+    def plain():
+        for j in range(plain_calls):
+            Y.mul(C1[j:j + 1], C2[j:j + 1], relin=True, out=o1)
+            torch.cuda.synchronize()
+    plain()
+    t0 = time.perf_counter()
+    plain()
+    plain_rate = plain_calls / (time.perf_counter() - t0)
+
+    # ---- polynomial products (Polynomial c = a*b; c.reduce()) ------------------
+    R = cy.Ring(N, Q_POLY)
+    PB = B
+    rng = np.random.default_rng(5)
+    A = torch.from_numpy((rng.integers(0, 2**63, size=(PB, N, L), dtype=np.uint64)).view(np.int64)).cuda()
+    Bp = torch.from_numpy((rng.integers(0, 2**63, size=(PB, N, L), dtype=np.uint64)).view(np.int64)).cuda()
+    A[..., 1] &= (1 << 62) - 1  # < 2^126 < q
+    Bp[..., 1] &= (1 << 62) - 1
+    Cp = R.empty(PB)
+    R.polymul(A, Bp, out=Cp)
+    poly_ms = time_steps(lambda: R.polymul(A, Bp, out=Cp), args.steps, stream)
+    poly_rate = PB * args.steps / (poly_ms / 1000.0)
+    c1p = R.empty(1)
+    t0 = time.perf_counter()
+    for j in range(plain_calls):
+        R.polymul(A[j:j + 1], Bp[j:j + 1], out=c1p)
+        torch.cuda.synchronize()
+    poly_plain = plain_calls / (time.perf_counter() - t0)
+
+    # ---- e2e: host buffers, copies inside the timed region ----------------------
+    H1 = C1.cpu().pin_memory()
+    H2 = C2.cpu().pin_memory()
+    HO = torch.empty_like(H1).pin_memory()
+    D1, D2 = torch.empty_like(C1), torch.empty_like(C2)
+
+    def e2e_step():
+        D1.copy_(H1, non_blocking=True)
+        D2.copy_(H2, non_blocking=True)
+        Y.mul(D1, D2, relin=True, out=OUT)
+        HO.copy_(OUT, non_blocking=True)
+
+    e2e_step()
+    e2e_ms = time_steps(e2e_step, max(2, args.steps // 2), stream)
+    e2e_rate = B * max(2, args.steps // 2) / (e2e_ms / 1000.0)
+    torch.cuda.synchronize()
+    e2e_ok = torch.equal(HO, OUT.cpu())
+
+    # ---- CPU baseline: the reference's multiply on the host cores ---------------
+    cpu = None
+    try:
+        threads = os.cpu_count() or 1
+        F, H, EV = Y.get_keys()
+        pairs = 8 * threads  # about 20 s of CPU work on a 16-core Grace
+        h1 = C1[:pairs].cpu().numpy().view(np.uint64)
+        h2 = C2[:pairs].cpu().numpy().view(np.uint64)
+        rate, secs = cpu_yashe_rate(pairs, threads, h1, h2, EV)
+        cpu = {"value": rate, "unit": "HE mults/s", "cores": threads, "kind": "port",
+               "sample": "%d HE multiplies at N=4096 with the reference's CPU multiply (C restatement), "
+                         "%.1f s wall on %d threads" % (pairs, secs, threads)}
+    except Exception as e:  # the baseline must not sink the GPU number
+        log("cpu baseline failed:", e)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "HE mults/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 ell=%d" % info.ell,
+                   "batch_pairs_per_gpu": B, "tensor_primes": info.tensor_primes, "relin_primes": info.relin_primes,
+                   "l2": "inputs larger than L2 (%.0f MB per step)" % (2 * B * CT_BYTES / 1e6),
+                   "parallelism": "replicas x%d" % world},
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_rate, "unit": "HE mults/s", "h2d_bytes_per_step": 2 * B * CT_BYTES,
+                "d2h_bytes_per_step": B * CT_BYTES, "output_matches_device": e2e_ok},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "step_roofline": {"bound": "hbm", "achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
+                          "frac": round(step_gbs / peak, 4), "algorithmic_bytes_per_step": step_bytes},
+        "kernels": kernels,
+        "plain_per_call": {"he_mults_per_s": plain_rate, "batched_over_plain": value / world / plain_rate},
+        "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
+                    "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
+        "decrypt_check": decrypt_ok,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=4096, help="ciphertext pairs per GPU per step")
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ncu-step", action="store_true",
+                    help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: warm-up raised to 3")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,10 @@ class YasheInfo(ctypes.Structure):
                 ("relin_primes", ctypes.c_int), ("has_keys", ctypes.c_int)]
 
 
+class TraceEntry(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
+
+
 class PolymulJob(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_void_p), ("d_a", ctypes.c_void_p), ("d_b", ctypes.c_void_p),
                 ("d_c", ctypes.c_void_p)]
@@ -101,6 +105,9 @@ SIGNATURES = {
     "cy_yashe_mul_ws": ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_launch_count": ([], ctypes.c_uint64),
+    "cy_trace_start": ([], _i),
+    "cy_trace_stop": ([ctypes.POINTER(TraceEntry), _i, ctypes.POINTER(_i)], _i),
 }
 
 _lib = None
@@ -148,6 +155,27 @@ def _ptr(t) -> int:
 
 def limbs_of(x: int, n: int):
     return (ctypes.c_uint64 * n)(*[(x >> (64 * i)) & 0xFFFFFFFFFFFFFFFF for i in range(n)])
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far."""
+    return int(lib().cy_launch_count())
+
+
+class Trace:
+    """Context manager: per-kernel launch counts and device time (CUDA events)."""
+
+    def __enter__(self):
+        check(lib().cy_trace_start(), "cy_trace_start")
+        self.kernels = {}
+        return self
+
+    def __exit__(self, *exc):
+        buf = (TraceEntry * 256)()
+        n = ctypes.c_int(0)
+        check(lib().cy_trace_stop(buf, 256, ctypes.byref(n)), "cy_trace_stop")
+        self.kernels = {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(min(n.value, 256))}
+        return False
 
 
 from .api import Ring, Yashe, Workspace  # noqa: E402,F401

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <set>
@@ -26,13 +27,24 @@ void* shoup_pairs_kernel();
 
 static constexpr int kEpiThreads = 256;
 
-static int default_chunk(int n) {
-    // jobs per launch: keep the residue scratch of a chunk around 32 MiB so it
-    // stays resident in L2 between the NTT kernel and the epilogue
-    long long per_job = (long long)n * 27 * 4;
-    long long c = (32ll << 20) / per_job;
+int trace_begin(const char* name, int logn, cudaStream_t st);
+void trace_end(int idx, cudaStream_t st);
+
+// Jobs per launch: the residue scratch of one chunk (k residues of N words per
+// job) is kept near CY_CHUNK_BYTES (default 32 MiB) so that it stays in L2
+// between the NTT kernel that writes it and the epilogue that reads it.
+static long long chunk_bytes() {
+    static long long v = [] {
+        const char* e = std::getenv("CY_CHUNK_BYTES");
+        long long x = e ? std::atoll(e) : 0;
+        return x > 0 ? x : (32ll << 20);
+    }();
+    return v;
+}
+static int chunk_jobs(int n, int k) {
+    long long c = chunk_bytes() / ((long long)n * k * 4);
     if (c < 1) c = 1;
-    if (c > 4096) c = 4096;
+    if (c > 65535) c = 65535;
     return (int)c;
 }
 
@@ -48,11 +60,19 @@ static cy_status ensure_smem(void* func, size_t bytes) {
     return CY_OK;
 }
 
-static cy_status launch(void* func, dim3 grid, dim3 block, size_t smem, cudaStream_t st, void** args) {
+static cy_status launch(void* func, const char* name, int logn, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                        void** args) {
     if (!func) return set_error(CY_ERR_INTERNAL, "missing kernel instantiation");
     CY_TRY(ensure_smem(func, smem));
-    CY_CUDA(cudaLaunchKernel(func, grid, block, args, smem, st));
+    const int tr = trace_begin(name, logn, st);
+    const cudaError_t e = cudaLaunchKernel(func, grid, block, args, smem, st);
+    trace_end(tr, st);
+    if (e != cudaSuccess) return cuda_error(e, name);
     return CY_OK;
+}
+
+static const char* epi_name(int mode) {
+    return mode == EPI_YASHE ? "epi_yashe" : mode == EPI_DECRYPT ? "epi_decrypt" : "epi_modq";
 }
 
 static cy_status check_device(int device) {
@@ -69,7 +89,7 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
     if (batch == 0) return CY_OK;
     const KernelSet& ks = kernel_set(B.h.logn);
     const int n = B.h.n, k = B.h.k;
-    const int chunk = std::min(batch, default_chunk(n));
+    const int chunk = std::min(batch, chunk_jobs(n, k));
     CY_TRY(ws.reserve((size_t)chunk * k * n));
     void* epi = epi_kernel(B.h.l32, B.h.mode);
     for (int j0 = 0; j0 < batch; j0 += chunk) {
@@ -79,12 +99,13 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
         const BasisDev* Bd = B.d;
         uint32_t* resid = ws.d_resid;
         void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
-        CY_TRY(launch(ks.mul[centered ? 1 : 0], dim3(k, nj), dim3(ks.threads), ks.smem_mul, st, args));
+        CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
+                      dim3(ks.threads), ks.smem_mul, st, args));
         void* oj = (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t);
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
-                      eargs));
+        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+                      dim3(kEpiThreads), 0, st, eargs));
     }
     return CY_OK;
 }
@@ -95,7 +116,7 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
     if (batch == 0) return CY_OK;
     const KernelSet& ks = kernel_set(B.h.logn);
     const int n = B.h.n, k = B.h.k, l64 = B.h.l64;
-    const int chunk = std::min(batch, default_chunk(n));
+    const int chunk = std::min(batch, chunk_jobs(n, k));
     CY_TRY(ws.reserve((size_t)chunk * k * n));
     int maxsm = 0, dev = 0;
     CY_CUDA(cudaGetDevice(&dev));
@@ -108,12 +129,13 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
         const BasisDev* Bd = B.d;
         uint32_t* resid = ws.d_resid;
         void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
-        CY_TRY(launch(ks.ks[sel], dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel], st, args));
+        CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel],
+                      st, args));
         uint64_t* oj = out + (size_t)j0 * n * l64;
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
-                      eargs));
+        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+                      dim3(kEpiThreads), 0, st, eargs));
     }
     return CY_OK;
 }
@@ -124,7 +146,7 @@ static cy_status run_crt(const Basis& B, const uint64_t* x, uint32_t* res, const
     const BasisDev* Bd = B.d;
     long long threads = (long long)batch * B.h.n;
     void* args[] = {(void*)&Bd, (void*)&x, (void*)&res, (void*)&d_scale, (void*)&batch};
-    return launch(crt_kernel(), dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st, args);
+    return launch(crt_kernel(), "crt", B.h.logn, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st, args);
 }
 
 static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st) {
@@ -137,7 +159,8 @@ static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse,
         int nj = std::min(65535, batch - j0);
         uint32_t* rj = res + (size_t)j0 * B.h.k * B.h.n;
         args[1] = (void*)&rj;
-        CY_TRY(launch(ks.ntt[inverse ? 1 : 0], dim3(B.h.k, nj), dim3(ks.threads), ks.smem_ntt, st, args));
+        CY_TRY(launch(ks.ntt[inverse ? 1 : 0], inverse ? "ntt_inv" : "ntt_fwd", B.h.logn, dim3(B.h.k, nj),
+                      dim3(ks.threads), ks.smem_ntt, st, args));
     }
     return CY_OK;
 }
@@ -148,18 +171,30 @@ static cy_status run_addsub(const cy_ring* r, const uint64_t* a, const uint64_t*
     long long count = (long long)batch * r->n;
     const uint64_t* q = r->d_q;
     void* args[] = {(void*)&a, (void*)&b, (void*)&c, (void*)&q, (void*)&count};
-    return launch(addsub_kernel(r->l64, sub), dim3((unsigned)((count + 255) / 256)), dim3(256), 0, st, args);
+    return launch(addsub_kernel(r->l64, sub), sub ? "polysub" : "polyadd", r->logn,
+                  dim3((unsigned)((count + 255) / 256)), dim3(256), 0, st, args);
+}
+
+// Buffers must be 16-byte aligned: the kernels load coefficients with 16-byte
+// vector loads (cudaMalloc returns 256-byte aligned memory).
+static cy_status check_aligned(const void* a, const void* b, const void* c) {
+    if (((uintptr_t)a | (uintptr_t)b | (uintptr_t)c) & 15)
+        return set_error(CY_ERR_INVALID_ARGUMENT, "buffers must be 16-byte aligned");
+    return CY_OK;
 }
 
 static cy_status validate_poly_args(const cy_ring* r, const void* a, const void* b, const void* c, int batch) {
     if (!r) return set_error(CY_ERR_INVALID_ARGUMENT, "ring is NULL");
     if (batch < 0) return set_error(CY_ERR_INVALID_ARGUMENT, "batch < 0");
     if (batch > 0 && (!a || !b || !c)) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL buffer");
+    CY_TRY(check_aligned(a, b, c));
     return check_device(r->device);
 }
 
 // bound = 4 * N * q^2: |X| < N q^2 for products of values in [0, q)
 static BigUInt product_bound(int n, const BigUInt& q) { return BigUInt(4ull * (uint64_t)n) * q * q; }
+
+cy_status check_aligned_api(const void* a, const void* b, const void* c) { return check_aligned(a, b, c); }
 
 cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
@@ -192,7 +227,8 @@ cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n,
         const BasisDev* Bd = relin.d;
         long long total = (long long)words;
         void* args[] = {(void*)&Bd, (void*)&d_res, (void*)&out, (void*)&total};
-        st = launch(shoup_pairs_kernel(), dim3((unsigned)((total + 255) / 256)), dim3(256), 0, 0, args);
+        st = launch(shoup_pairs_kernel(), "shoup_pairs", relin.h.logn, dim3((unsigned)((total + 255) / 256)), dim3(256),
+                    0, 0, args);
     }
     if (st == CY_OK) {
         e = cudaDeviceSynchronize();
@@ -364,7 +400,7 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
         scale[2 * i + 1] = (uint32_t)(((uint64_t)v << 32) / p);
     }
     cudaStream_t st = (cudaStream_t)stream;
-    const int chunk = std::min(batch, default_chunk(n));
+    const int chunk = std::min(batch, chunk_jobs(n, k));
     Workspace& ws = r->own_ws.ws;
     CY_TRY(ws.reserve((size_t)chunk * k * n + 2 * (size_t)KMAX));
     uint32_t* d_scale = ws.d_resid + (size_t)chunk * k * n;
@@ -379,8 +415,8 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
         uint64_t* oj = d_c + (size_t)j0 * n * r->l64;
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0, st,
-                      eargs));
+        CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+                      dim3(kEpiThreads), 0, st, eargs));
     }
     // the scale vector is read by the kernels above before the stream moves on
     return CY_OK;
@@ -426,8 +462,8 @@ cy_status cy_icrt(cy_ring* r, const uint32_t* d_res, uint64_t* d_x, int batch, c
         uint64_t* xj = d_x + (size_t)j0 * r->n * r->l64;
         void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj};
         long long threads = (long long)nj * r->n;
-        CY_TRY(launch(epi, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)), dim3(kEpiThreads), 0,
-                      (cudaStream_t)stream, eargs));
+        CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+                      dim3(kEpiThreads), 0, (cudaStream_t)stream, eargs));
     }
     return CY_OK;
 }

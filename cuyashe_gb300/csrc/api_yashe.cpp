@@ -17,6 +17,7 @@
 #include "host.h"
 
 namespace cy {
+cy_status check_aligned_api(const void* a, const void* b, const void* c);
 cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
                           cudaStream_t st);
@@ -41,6 +42,7 @@ static cy_status yashe_check(const cy_yashe* y, const void* a, const void* b, in
     if (!y) return set_error(CY_ERR_INVALID_ARGUMENT, "yashe handle is NULL");
     if (batch < 0) return set_error(CY_ERR_INVALID_ARGUMENT, "batch < 0");
     if (batch > 0 && (!a || !b)) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL buffer");
+    CY_TRY(check_aligned_api(a, b, nullptr));
     int cur = -1;
     CY_CUDA(cudaGetDevice(&cur));
     if (cur != y->ring->device) return set_error(CY_ERR_INVALID_ARGUMENT, "handle belongs to another CUDA device");
@@ -173,6 +175,7 @@ cy_status cy_yashe_mul_ws(cy_yashe* y, cy_workspace* ws, const uint64_t* d_c1, c
                           uint64_t* d_out, int batch, int relin, cy_stream_t stream) {
     CY_TRY(yashe_check(y, d_c1, d_c2, batch));
     if (batch > 0 && !d_out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL buffer");
+    CY_TRY(check_aligned_api(d_out, nullptr, nullptr));
     if (relin && !y->has_keys) return set_error(CY_ERR_NO_KEYS, "relinearisation needs keys");
     cy_ring* r = y->ring;
     const long long stride = (long long)r->n * r->l64;

@@ -7,12 +7,16 @@
 
 namespace cy {
 
+// [l64][...]: index 0 holds the generic kernels (limb count read at run time),
+// index L64 the kernels specialised for coefficients of L64 limbs (or null).
 struct KernelSet {
     int logn = 0, loge = 0, threads = 0;
-    void* mul[2] = {nullptr, nullptr};  // [centered]
-    void* ks[2] = {nullptr, nullptr};   // keyswitch with 2 / 4 digits per pass
+    void* mul[7][2] = {};  // [l64][centered]
+    void* ks[7][2] = {};   // [l64][keyswitch with 2 / 4 digits per pass]
     void* ntt[2] = {nullptr, nullptr};  // forward / inverse
     size_t smem_mul = 0, smem_ks[2] = {0, 0}, smem_ntt = 0;
+    void* mul_for(int l64, bool centered) const { return mul[mul[l64][0] ? l64 : 0][centered ? 1 : 0]; }
+    void* ks_for(int l64, int nd4) const { return ks[ks[l64][0] ? l64 : 0][nd4]; }
 };
 
 // Kernel set for transforms of length 2^logn (1 <= logn <= LOGN_MAX).

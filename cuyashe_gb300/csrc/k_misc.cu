@@ -6,7 +6,8 @@
 namespace cy {
 
 void fill_small(KernelSet* t);
-void fill_n10_11(KernelSet* t);
+void fill_n10(KernelSet* t);
+void fill_n11(KernelSet* t);
 void fill_n12(KernelSet* t);
 void fill_n13(KernelSet* t);
 void fill_n14(KernelSet* t);
@@ -16,7 +17,8 @@ const KernelSet& kernel_set(int logn) {
     static std::once_flag once;
     std::call_once(once, [] {
         fill_small(table);
-        fill_n10_11(table);
+        fill_n10(table);
+        fill_n11(table);
         fill_n12(table);
         fill_n13(table);
         fill_n14(table);
@@ -64,9 +66,7 @@ __global__ void k_shoup_pairs(const BasisDev* __restrict__ B, const uint32_t* __
                               long long total) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= total) return;
-    const int n = 1 << B->logn;
     const int prime = (int)((idx >> B->logn) % B->k);
-    (void)n;
     const uint32_t p = B->p[prime];
     const uint32_t x = v[idx];
     out[idx] = make_uint2(x, (uint32_t)(((uint64_t)x << 32) / p));

@@ -87,11 +87,59 @@ __device__ __forceinline__ uint32_t crt_coef(const uint64_t* __restrict__ src, i
     return acc;
 }
 
+// The limbs of one coefficient as 32-bit words (16-byte loads when L64 is even).
+template <int L64>
+__device__ __forceinline__ void load_words(const uint64_t* __restrict__ p, uint32_t (&w)[2 * L64]) {
+    if constexpr (L64 % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < L64 / 2; i++) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
+            w[4 * i] = v.x;
+            w[4 * i + 1] = v.y;
+            w[4 * i + 2] = v.z;
+            w[4 * i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < L64; i++) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(p) + i);
+            w[2 * i] = v.x;
+            w[2 * i + 1] = v.y;
+        }
+    }
+}
+
+// Residue in [0, 4p) of the coefficient whose 32-bit words are w (compile-time
+// count W); cc[j] = 2^(32 j) mod p. With CENTER, values above (q-1)/2 (words
+// qh) stand for x - q.
+template <int W, bool CENTER>
+__device__ __forceinline__ uint32_t crt_words(const uint32_t (&w)[W], const uint32_t (&cc)[W],
+                                              const uint32_t (&qh)[W], const PrimeCtx& c) {
+    uint32_t acc = 0;
+#pragma unroll
+    for (int j0 = 0; j0 < W; j0 += 4) {
+        uint64_t T = 0;
+#pragma unroll
+        for (int j = j0; j < j0 + 4 && j < W; j++) T += (uint64_t)w[j] * cc[j];  // < 4 * 2^62
+        const uint32_t f = fold64(T, c);
+        acc = (j0 == 0) ? f : red(acc + f, 2 * c.p);
+    }
+    if (CENTER) {
+        bool gt = false;
+#pragma unroll
+        for (int j = 0; j < W; j++) gt = (w[j] > qh[j]) || (w[j] == qh[j] && gt);
+        if (gt) acc = acc + 2 * c.p - c.qmodp;  // [0, 4p)
+    }
+    return acc;
+}
+
 // --------------------------------------------------------------------------
 // k_mul: one block per (prime, job); G = N/E threads
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, bool CENTER>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+// L64 > 0: coefficients have exactly L64 limbs (specialised load and CRT
+// split); L64 == 0: the limb count is read from the basis at run time.
+template <int LOGN, int LOGE, int L64, bool CENTER>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G <= 512 ? 3 : 1)
     k_mul(const BasisDev* __restrict__ B, const uint64_t* __restrict__ A, long long a_stride,
           const uint64_t* __restrict__ Bv, long long b_stride, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -115,11 +163,30 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
     const uint64_t* a = A + (size_t)job * a_stride;
     const uint64_t* b = Bv + (size_t)job * b_stride;
     uint32_t x[2][E];
+    if constexpr (L64 > 0) {
+        constexpr int W = 2 * L64;
+        uint32_t cc[W], qh[W];
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-        const int pos = slot_pos<PL, 0>(tau, e);
-        x[0][e] = crt_coef<CENTER>(a, pos, l64, s_crt, s_qhalf, c);
-        x[1][e] = crt_coef<CENTER>(b, pos, l64, s_crt, s_qhalf, c);
+        for (int j = 0; j < W; j++) {
+            cc[j] = s_crt[j];
+            qh[j] = s_qhalf[j];
+        }
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int pos = slot_pos<PL, 0>(tau, e);
+            uint32_t wa[W], wb[W];
+            load_words<L64>(a + (size_t)pos * L64, wa);
+            load_words<L64>(b + (size_t)pos * L64, wb);
+            x[0][e] = crt_words<W, CENTER>(wa, cc, qh, c);
+            x[1][e] = crt_words<W, CENTER>(wb, cc, qh, c);
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int pos = slot_pos<PL, 0>(tau, e);
+            x[0][e] = crt_coef<CENTER>(a, pos, l64, s_crt, s_qhalf, c);
+            x[1][e] = crt_coef<CENTER>(b, pos, l64, s_crt, s_qhalf, c);
+        }
     }
     constexpr int STRIDE = region_stride<PL, 2>();
     int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0);
@@ -137,8 +204,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 // coefficients of c in [0, q) (w = 2^32), processed ND at a time.
 // evk: [ell][k][N] (value, Shoup companion) in the forward-NTT output order.
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, int ND>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+template <int LOGN, int LOGE, int L64, int ND>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G <= 512 ? 2 : 1)
     k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
                 int ell, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -148,7 +215,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
     const int tau = threadIdx.x;
     const int prime = blockIdx.x;
     const int job = blockIdx.y;
-    const int k = B->k, l64 = B->l64;
+    const int k = B->k, l64 = L64 > 0 ? L64 : B->l64;
     const uint32_t p = B->p[prime];
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
@@ -164,15 +231,38 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int pos = slot_pos<PL, 0>(tau, e);
+            if constexpr (L64 > 0 && ND % 2 == 0) {
+                // digits d0 .. d0+ND-1 are limbs d0/2 .. d0/2+ND/2-1 of the coefficient;
+                // digits past the last word of q are zero (coefficients are < q)
+                const uint64_t* src = cj + (size_t)pos * L64 + (d0 >> 1);
+                uint32_t w[ND];
+                if constexpr (ND == 4 && L64 % 2 == 0) {
+                    const uint4 v = __ldg(reinterpret_cast<const uint4*>(src));
+                    w[0] = v.x;
+                    w[1] = v.y;
+                    w[2] = v.z;
+                    w[3] = v.w;
+                } else {
 #pragma unroll
-            for (int o = 0; o < ND; o++) {
-                const int d = d0 + o;
-                uint32_t w = 0;
-                if (d < ell) {
-                    const uint64_t limb = __ldg(cj + (size_t)pos * l64 + (d >> 1));
-                    w = (uint32_t)(limb >> (32 * (d & 1)));
+                    for (int o = 0; o < ND; o += 2) {
+                        const uint2 v = __ldg(reinterpret_cast<const uint2*>(src) + (o >> 1));
+                        w[o] = v.x;
+                        w[o + 1] = v.y;
+                    }
                 }
-                x[o][e] = red(w, 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
+#pragma unroll
+                for (int o = 0; o < ND; o++) x[o][e] = red(w[o], 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
+            } else {
+#pragma unroll
+                for (int o = 0; o < ND; o++) {
+                    const int d = d0 + o;
+                    uint32_t w = 0;
+                    if (d < ell) {
+                        const uint64_t limb = __ldg(cj + (size_t)pos * l64 + (d >> 1));
+                        w = (uint32_t)(limb >> (32 * (d & 1)));
+                    }
+                    x[o][e] = red(w, 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
+                }
             }
         }
         buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf);
@@ -423,16 +513,29 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
 
 namespace cy {
 
-template <int LOGN, int LOGE>
+template <int LOGN, int LOGE, int L64>
+void fill_l64(KernelSet& ks) {
+    ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false>;
+    ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true>;
+    ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, 2>;
+    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4>;
+}
+
+// SPECIALISE: also instantiate the kernels for 1, 2, 3 and 6 limbs (q of up to
+// 64, 128, 192 and 384 bits); other limb counts use the generic kernels.
+template <int LOGN, int LOGE, bool SPECIALISE>
 void fill_kernel_set(KernelSet& ks) {
     using PL = NttPlan<LOGN, LOGE>;
     ks.logn = LOGN;
     ks.loge = LOGE;
     ks.threads = PL::G;
-    ks.mul[0] = (void*)k_mul<LOGN, LOGE, false>;
-    ks.mul[1] = (void*)k_mul<LOGN, LOGE, true>;
-    ks.ks[0] = (void*)k_keyswitch<LOGN, LOGE, 2>;
-    ks.ks[1] = (void*)k_keyswitch<LOGN, LOGE, 4>;
+    fill_l64<LOGN, LOGE, 0>(ks);
+    if constexpr (SPECIALISE) {
+        fill_l64<LOGN, LOGE, 1>(ks);
+        fill_l64<LOGN, LOGE, 2>(ks);
+        fill_l64<LOGN, LOGE, 3>(ks);
+        fill_l64<LOGN, LOGE, 6>(ks);
+    }
     ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
     ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
     ks.smem_mul = region_bytes<PL, 2>();

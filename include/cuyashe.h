@@ -210,6 +210,28 @@ cy_status cy_yashe_keyswitch(cy_yashe *y, const uint64_t *d_c, uint64_t *d_out, 
 cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out, int batch,
                        cy_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Observability                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Kernels launched by this library since the process started. The reference
+ * has no launch accounting; its timing is rdtsc/clock_gettime around whole
+ * operations (src/common.cpp:15-59). */
+uint64_t cy_launch_count(void);
+
+/* Per-kernel tracing: between cy_trace_start and cy_trace_stop every launch is
+ * bracketed by CUDA events recorded on the launch stream. cy_trace_stop
+ * synchronises those events and returns, per kernel name, the number of
+ * launches and the summed device time. Tracing adds two event records per
+ * launch; leave it off in timed regions. */
+typedef struct cy_trace_entry {
+    char name[48];
+    int launches;
+    double total_ms;
+} cy_trace_entry;
+cy_status cy_trace_start(void);
+cy_status cy_trace_stop(cy_trace_entry *entries, int max_entries, int *n_entries);
+
 #ifdef __cplusplus
 }
 #endif
