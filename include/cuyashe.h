@@ -120,6 +120,25 @@ cy_status cy_polysub(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, ui
 cy_status cy_poly_scalar_mul(cy_ring *ring, const uint64_t *d_a, const uint64_t *h_scalar, uint64_t *d_c,
                              int batch, cy_stream_t stream);
 
+/* The product c = a*b mod (x^N+1, q), like cy_polymul, for callers that must
+ * not allocate device memory: code that records work into a CUDA graph
+ * (cudaMalloc is refused while a stream is being captured), latency-critical
+ * or serving paths that cannot take cudaMalloc's device-wide synchronisation,
+ * and hosts whose device memory is owned by another allocator or a fixed
+ * budget. It calls no cudaMalloc, cudaFree or allocating library routine: its
+ * scratch is a fixed array of CY_NOALLOC_SCRATCH_BYTES in the library's device
+ * image, held by every GPU that loads the library until the process exits.
+ * Limit: batch * (CRT primes) * N * 4 bytes must fit in that array (at N = 4096
+ * and a 127-bit q, 113 products per call); larger batches are rejected with
+ * CY_ERR_INVALID_ARGUMENT and a message giving the maximum. The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. All calls share the array, so
+ * calls that can overlap on the GPU race and must be serialised by the caller.
+ * This entry point has no counterpart in the reference. */
+#define CY_NOALLOC_SCRATCH_BYTES (16u << 20)
+cy_status cy_polymul_noalloc(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
+                             cy_stream_t stream);
+
 /* Mixed batch: products of different rings (different N and q) in one
  * submission. Jobs are grouped by ring and launched back to back on `stream`. */
 typedef struct cy_polymul_job {
