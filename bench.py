@@ -231,9 +231,12 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     B = args.batch
 
-    # ---- set-up (untimed): keys, fresh encryptions, correctness check --------
+    # ---- set-up (untimed): keys, schedule autotuning, fresh encryptions --------
     Y = cy.Yashe(N, Q_YASHE, T, W_BITS, 8.0)
     Y.keygen(1234 + rank)
+    if not args.no_autotune:
+        Y.autotune(batch=512)
+    tuning = cy.tuning_export()
     C1, C2, m1, m2, idx1, idx2 = make_inputs(Y, B, pool=32, seed=77 + rank)
     OUT = Y.ring.empty(B)
     Y.mul(C1, C2, relin=True, out=OUT)
@@ -323,6 +326,8 @@ def run_ours(args):
 
     # ---- polynomial products (Polynomial c = a*b; c.reduce()) ------------------
     R = cy.Ring(N, Q_POLY)
+    if not args.no_autotune:
+        R.autotune(batch=512)
     PB = B
     rng = np.random.default_rng(5)
     A = torch.from_numpy((rng.integers(0, 2**63, size=(PB, N, L), dtype=np.uint64)).view(np.int64)).cuda()
@@ -380,7 +385,7 @@ def run_ours(args):
         "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 ell=%d" % info.ell,
                    "batch_pairs_per_gpu": B, "tensor_primes": info.tensor_primes, "relin_primes": info.relin_primes,
                    "l2": "inputs larger than L2 (%.0f MB per step)" % (2 * B * CT_BYTES / 1e6),
-                   "parallelism": "replicas x%d" % world},
+                   "parallelism": "replicas x%d" % world, "schedules": tuning},
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_rate, "unit": "HE mults/s", "h2d_bytes_per_step": 2 * B * CT_BYTES,
                 "d2h_bytes_per_step": B * CT_BYTES, "output_matches_device": e2e_ok},
@@ -408,6 +413,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=4096, help="ciphertext pairs per GPU per step")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT schedules")
     ap.add_argument("--ncu-step", action="store_true",
                     help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
     args = ap.parse_args()

@@ -106,6 +106,10 @@ SIGNATURES = {
     "cy_yashe_mul_ws": ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_ring_autotune": ([_vp, _i, _vp], _i),
+    "cy_yashe_autotune": ([_vp, _i, _vp], _i),
+    "cy_tuning_export": ([ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], _i),
+    "cy_tuning_import": ([ctypes.c_char_p], _i),
     "cy_launch_count": ([], ctypes.c_uint64),
     "cy_trace_start": ([], _i),
     "cy_trace_stop": ([ctypes.POINTER(TraceEntry), _i, ctypes.POINTER(_i)], _i),
@@ -156,6 +160,19 @@ def _ptr(t) -> int:
 
 def limbs_of(x: int, n: int):
     return (ctypes.c_uint64 * n)(*[(x >> (64 * i)) & 0xFFFFFFFFFFFFFFFF for i in range(n)])
+
+
+def tuning_export() -> str:
+    """The autotuner's choices for the current device ("n4096.l2.mul=1;...")."""
+    need = ctypes.c_size_t(0)
+    check(lib().cy_tuning_export(None, 0, ctypes.byref(need)), "cy_tuning_export")
+    buf = ctypes.create_string_buffer(need.value + 1)
+    check(lib().cy_tuning_export(buf, len(buf), ctypes.byref(need)), "cy_tuning_export")
+    return buf.value.decode()
+
+
+def tuning_import(spec: str) -> None:
+    check(lib().cy_tuning_import(spec.encode()), "cy_tuning_import")
 
 
 def launch_count() -> int:

@@ -143,6 +143,9 @@ class Ring:
                                        _stream_handle(stream)), "cy_poly_scalar_mul")
         return out
 
+    def autotune(self, batch: int = 256, stream=None) -> None:
+        check(lib().cy_ring_autotune(self.h, batch, _stream_handle(stream)), "cy_ring_autotune")
+
     def residues_empty(self, batch: int):
         import torch
         return torch.empty((batch, self.k, self.n), dtype=torch.int32, device="cuda")
@@ -202,6 +205,9 @@ class Yashe:
     @property
     def ell(self) -> int:
         return self.info().ell
+
+    def autotune(self, batch: int = 256, stream=None) -> None:
+        check(lib().cy_yashe_autotune(self.h, batch, _stream_handle(stream)), "cy_yashe_autotune")
 
     def keygen(self, seed: int) -> None:
         check(lib().cy_yashe_keygen(self.h, seed), "cy_yashe_keygen")

@@ -82,12 +82,16 @@ static cy_status check_device(int device) {
     return CY_OK;
 }
 
-// products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j)
+int tuned_variant(int logn, int l64, int op);
+
+// products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j); `variant`
+// selects the NTT schedule (-1: the tuned one for this device and size)
 static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, long long a_stride,
                              const uint64_t* b, long long b_stride, void* out, long long out_stride, int batch,
-                             Workspace& ws, cudaStream_t st) {
+                             Workspace& ws, cudaStream_t st, int variant = -1) {
     if (batch == 0) return CY_OK;
-    const KernelSet& ks = kernel_set(B.h.logn);
+    const KernelSet& ks = kernel_variant(
+        B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, centered ? TUNE_MULC : TUNE_MUL));
     const int n = B.h.n, k = B.h.k;
     const int chunk = std::min(batch, chunk_jobs(n, k));
     CY_TRY(ws.reserve((size_t)chunk * k * n));
@@ -112,9 +116,10 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
 
 // keyswitch of `batch` polynomials c_j -> out_j (may alias c)
 static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out,
-                               int batch, Workspace& ws, cudaStream_t st) {
+                               int batch, Workspace& ws, cudaStream_t st, int variant = -1) {
     if (batch == 0) return CY_OK;
-    const KernelSet& ks = kernel_set(B.h.logn);
+    const KernelSet& ks =
+        kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_KS));
     const int n = B.h.n, k = B.h.k, l64 = B.h.l64;
     const int chunk = std::min(batch, chunk_jobs(n, k));
     CY_TRY(ws.reserve((size_t)chunk * k * n));
@@ -198,13 +203,13 @@ cy_status check_aligned_api(const void* a, const void* b, const void* c) { retur
 
 cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
-                          cudaStream_t st) {
-    return run_product(B, centered, a, a_stride, b, b_stride, out, out_stride, batch, ws, st);
+                          cudaStream_t st, int variant) {
+    return run_product(B, centered, a, a_stride, b, b_stride, out, out_stride, batch, ws, st, variant);
 }
 
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st) {
-    return run_keyswitch(B, c, evk, ell, out, batch, ws, st);
+                            Workspace& ws, cudaStream_t st, int variant) {
+    return run_keyswitch(B, c, evk, ell, out, batch, ws, st, variant);
 }
 
 // Evaluation key in the keyswitch basis, NTT domain, with Shoup companions:

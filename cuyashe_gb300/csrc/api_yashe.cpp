@@ -20,9 +20,9 @@ namespace cy {
 cy_status check_aligned_api(const void* a, const void* b, const void* c);
 cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
-                          cudaStream_t st);
+                          cudaStream_t st, int variant = -1);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st);
+                            Workspace& ws, cudaStream_t st, int variant = -1);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 cy_status host_keygen(cy_yashe* y, uint64_t seed, std::vector<uint64_t>& f, std::vector<uint64_t>& h,
                       std::vector<uint64_t>& evk);

@@ -19,8 +19,16 @@ struct KernelSet {
     void* ks_for(int l64, int nd4) const { return ks[ks[l64][0] ? l64 : 0][nd4]; }
 };
 
-// Kernel set for transforms of length 2^logn (1 <= logn <= LOGN_MAX).
+// Kernel sets for transforms of length 2^logn (1 <= logn <= LOGN_MAX). Each
+// length has one or more schedules ("variants": coefficients per thread, hence
+// threads per transform and passes); variant 0 is the default, the autotuner
+// may pick another per ring (tuning.cpp).
 const KernelSet& kernel_set(int logn);
+int variant_count(int logn);
+const KernelSet& kernel_variant(int logn, int v);
+
+// Tuned operations (keys of the autotuner's table).
+enum TuneOp { TUNE_MUL = 0, TUNE_MULC = 1, TUNE_KS = 2, TUNE_OPS = 3 };
 
 // ICRT epilogue for `l32` words of q and epilogue mode (EpiMode).
 void* epi_kernel(int l32, int mode);

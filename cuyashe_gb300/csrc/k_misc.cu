@@ -1,30 +1,58 @@
 // ICRT epilogues, CRT split, elementwise mod-q kernels and the dispatch tables.
 #include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 
 namespace cy {
 
 void fill_small(KernelSet* t);
-void fill_n10(KernelSet* t);
-void fill_n11(KernelSet* t);
-void fill_n12(KernelSet* t);
-void fill_n13(KernelSet* t);
-void fill_n14(KernelSet* t);
+void fill_n10_e3(KernelSet& ks);
+void fill_n10_e4(KernelSet& ks);
+void fill_n11_e3(KernelSet& ks);
+void fill_n11_e4(KernelSet& ks);
+void fill_n12_e3(KernelSet& ks);
+void fill_n12_e4(KernelSet& ks);
+void fill_n13_e3(KernelSet& ks);
+void fill_n13_e4(KernelSet& ks);
+void fill_n14_e4(KernelSet& ks);
 
-const KernelSet& kernel_set(int logn) {
-    static KernelSet table[LOGN_MAX + 1];
+struct VariantTable {
+    std::vector<KernelSet> v[LOGN_MAX + 1];
+};
+
+static const VariantTable& variants() {
+    static VariantTable T;
     static std::once_flag once;
     std::call_once(once, [] {
-        fill_small(table);
-        fill_n10(table);
-        fill_n11(table);
-        fill_n12(table);
-        fill_n13(table);
-        fill_n14(table);
+        KernelSet small[LOGN_MAX + 1];
+        fill_small(small);
+        for (int logn = 1; logn <= 9; logn++) T.v[logn].push_back(small[logn]);
+        auto add = [](int logn, void (*fill)(KernelSet&)) {
+            KernelSet ks;
+            fill(ks);
+            T.v[logn].push_back(ks);
+        };
+        // variant 0 first: the default schedule of each length
+        add(10, fill_n10_e3);
+        add(10, fill_n10_e4);
+        add(11, fill_n11_e3);
+        add(11, fill_n11_e4);
+        add(12, fill_n12_e3);
+        add(12, fill_n12_e4);
+        add(13, fill_n13_e4);
+        add(13, fill_n13_e3);
+        add(14, fill_n14_e4);
     });
-    return table[logn];
+    return T;
 }
+
+int variant_count(int logn) { return (logn >= 1 && logn <= LOGN_MAX) ? (int)variants().v[logn].size() : 0; }
+const KernelSet& kernel_variant(int logn, int v) {
+    const std::vector<KernelSet>& vs = variants().v[logn];
+    return vs[(v >= 0 && v < (int)vs.size()) ? v : 0];
+}
+const KernelSet& kernel_set(int logn) { return kernel_variant(logn, 0); }
 
 #define CY_EPI_ROW(L) {(void*)k_epi<L, EPI_MODQ>, (void*)k_epi<L, EPI_YASHE>, (void*)k_epi<L, EPI_DECRYPT>}
 

@@ -138,8 +138,23 @@ __device__ __forceinline__ uint32_t crt_words(const uint32_t (&w)[W], const uint
 // --------------------------------------------------------------------------
 // L64 > 0: coefficients have exactly L64 limbs (specialised load and CRT
 // split); L64 == 0: the limb count is read from the basis at run time.
+// Blocks per SM the product kernel is compiled for: 48 resident warps with 8
+// coefficients per thread, 32 with 16 (more registers per thread).
+template <int LOGN, int LOGE>
+constexpr int mul_min_blocks() {
+    constexpr int G = NttPlan<LOGN, LOGE>::G;
+    constexpr int target = (LOGE <= 3 ? 1536 : 1024) / G;
+    return target < 1 ? 1 : (target > 16 ? 16 : target);
+}
+template <int LOGN, int LOGE>
+constexpr int ks_min_blocks() {
+    constexpr int G = NttPlan<LOGN, LOGE>::G;
+    constexpr int target = 1024 / G;
+    return target < 1 ? 1 : (target > 16 ? 16 : target);
+}
+
 template <int LOGN, int LOGE, int L64, bool CENTER>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G <= 512 ? 3 : 1)
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (mul_min_blocks<LOGN, LOGE>()))
     k_mul(const BasisDev* __restrict__ B, const uint64_t* __restrict__ A, long long a_stride,
           const uint64_t* __restrict__ Bv, long long b_stride, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -205,7 +220,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G
 // evk: [ell][k][N] (value, Shoup companion) in the forward-NTT output order.
 // --------------------------------------------------------------------------
 template <int LOGN, int LOGE, int L64, int ND>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G <= 512 ? 2 : 1)
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (ks_min_blocks<LOGN, LOGE>()))
     k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
                 int ell, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -271,10 +286,21 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, NttPlan<LOGN, LOGE>::G
             const int d = d0 + o;
             if (d < ell) {
                 const uint2* __restrict__ g = evk + ((size_t)d * k + prime) * PL::N;
+                if constexpr (PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE) {
+                    // after the last pass a thread's E positions are contiguous: 16-byte loads
+                    const uint4* g4 = reinterpret_cast<const uint4*>(g + group_base<PL, LAST>(tau, 0));
 #pragma unroll
-                for (int e = 0; e < E; e++) {
-                    const uint2 W = __ldg(g + slot_pos<PL, LAST>(tau, e));
-                    acc[0][e] = red(acc[0][e] + shoup(x[o][e], W.x, W.y, p), 2 * p);
+                    for (int h = 0; h < E / 2; h++) {
+                        const uint4 W = __ldg(g4 + h);
+                        acc[0][2 * h] = red(acc[0][2 * h] + shoup(x[o][2 * h], W.x, W.y, p), 2 * p);
+                        acc[0][2 * h + 1] = red(acc[0][2 * h + 1] + shoup(x[o][2 * h + 1], W.z, W.w, p), 2 * p);
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < E; e++) {
+                        const uint2 W = __ldg(g + slot_pos<PL, LAST>(tau, e));
+                        acc[0][e] = red(acc[0][e] + shoup(x[o][e], W.x, W.y, p), 2 * p);
+                    }
                 }
             }
         }
@@ -448,19 +474,38 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
     c0.zero();
     c1.zero();
     uint64_t vacc = 0;
-    int pending = 0;
-    for (int i = 0; i < k; i++) {
-        const uint32_t r = __ldcg(r0 + (size_t)i * n);
+    // One prime's contribution: y = [X Mhat_i^-1]_{p_i}, the fixed-point estimate
+    // of y/p_i for v, and y times the row(s) of constants into the columns.
+    auto absorb = [&](int i, uint32_t r) {
         const uint32_t p = S.p[i];
-        const uint32_t y = red(shoup(r, S.ycon[i], S.ycon_sh[i], p), p);  // [X Mhat_i^-1]_{p_i}
-        vacc += (uint64_t)y * S.fhi[i] + __umulhi(y, S.flo[i]);          // sum y_i/p_i in 2^-32 units
+        const uint32_t y = red(shoup(r, S.ycon[i], S.ycon_sh[i], p), p);
+        vacc += (uint64_t)y * S.fhi[i] + __umulhi(y, S.flo[i]);  // sum y_i/p_i in 2^-32 units
         c0.mac(y, &S.A0[i * L]);
         if (MODE == EPI_YASHE) c1.mac(y, &S.A1[i * L]);
-        if (++pending == 3) {
+    };
+    // Issue the loads of the first KU residues together (they come from L2), then
+    // absorb them; columns take three products of < 2^62 between carry passes.
+    constexpr int KU = 15;
+    uint32_t rk[KU];
+#pragma unroll
+    for (int i = 0; i < KU; i++) rk[i] = (i < k) ? __ldcg(r0 + (size_t)i * n) : 0u;
+#pragma unroll
+    for (int i = 0; i < KU; i++) {
+        if (i < k) absorb(i, rk[i]);
+        if (i % 3 == 2) {
             c0.norm();
             if (MODE == EPI_YASHE) c1.norm();
-            pending = 0;
         }
+    }
+    for (int i0 = KU; i0 < k; i0 += 3) {  // bases of more than KU primes
+        uint32_t rr[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) rr[j] = (i0 + j < k) ? __ldcg(r0 + (size_t)(i0 + j) * n) : 0u;
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            if (i0 + j < k) absorb(i0 + j, rr[j]);
+        c0.norm();
+        if (MODE == EPI_YASHE) c1.norm();
     }
     const uint32_t v = (uint32_t)((vacc + 0x80000000ULL) >> 32);  // round(sum y_i/p_i): X = sum y_i Mhat_i - v M
     c0.norm();

@@ -1,0 +1,260 @@
+// tuning.cpp -- choice of NTT schedule per (device, N, limb count, operation).
+//
+// Every transform length has one or more compiled schedules (kernel variants:
+// 8 or 16 coefficients per thread, hence 512/256/... threads per transform and
+// 4 or 3 register passes at N = 4096). The autotuner runs each schedule of an
+// operation on a synthetic batch of the caller's ring, checks that its output is
+// bit-identical to the default schedule's, times it with CUDA events and keeps
+// the fastest. Choices live in a process-wide table and can be exported and
+// imported as text ("n4096.l2.mul=1;n4096.l2.ks=0;...") so that a serving
+// process tunes once. The reference has a single fixed launch shape per kernel
+// (e.g. src/cuda_functions.cu:447-458) and commented-out block-size notes
+// (src/cuda_bn.cu:983-988, 1014-1019).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "host.h"
+
+namespace cy {
+
+cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
+                          long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
+                          cudaStream_t st, int variant);
+cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
+                            Workspace& ws, cudaStream_t st, int variant);
+cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
+
+static const char* kOpNames[TUNE_OPS] = {"mul", "mulc", "ks"};
+
+static std::mutex g_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_choice;  // (device, logn, l64, op) -> variant
+
+int tuned_variant(int logn, int l64, int op) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_choice.find(std::make_tuple(dev, logn, l64, op));
+    return it == g_choice.end() ? 0 : it->second;
+}
+
+static void set_choice(int dev, int logn, int l64, int op, int v) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_choice[std::make_tuple(dev, logn, l64, op)] = v;
+}
+
+// values < q: random words below the top bit of q
+static std::vector<uint64_t> random_polys(int count, int n, int l64, int qbits, uint64_t seed) {
+    std::vector<uint64_t> v((size_t)count * n * l64);
+    uint64_t s = seed;
+    for (auto& x : v) {
+        s += 0x9E3779B97F4A7C15ULL;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        x = z ^ (z >> 31);
+    }
+    const int top = (qbits - 2) % 64 + 1;  // bits kept in the top limb: value < 2^(qbits-1) <= q
+    const int toplimb = (qbits - 2) / 64;
+    for (size_t i = 0; i < v.size(); i += l64) {
+        for (int j = toplimb + 1; j < l64; j++) v[i + j] = 0;
+        if (top < 64) v[i + toplimb] &= (1ull << top) - 1;
+    }
+    return v;
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+// Time each schedule of one operation; `run(v, out)` launches it on `st`.
+template <class Run>
+static cy_status tune_op(int logn, int l64, int op, size_t out_bytes, cudaStream_t st, Run run, int* chosen) {
+    const int nv = variant_count(logn);
+    int dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    *chosen = 0;
+    if (nv <= 1) {
+        set_choice(dev, logn, l64, op, 0);
+        return CY_OK;
+    }
+    DevBuf ref, cur;
+    CY_CUDA(cudaMalloc(&ref.p, out_bytes));
+    CY_CUDA(cudaMalloc(&cur.p, out_bytes));
+    std::vector<unsigned char> h_ref(out_bytes), h_cur(out_bytes);
+    cudaEvent_t e0, e1;
+    CY_CUDA(cudaEventCreate(&e0));
+    CY_CUDA(cudaEventCreate(&e1));
+    float best = 0;
+    int best_v = 0;
+    cy_status st_all = CY_OK;
+    for (int v = 0; v < nv && st_all == CY_OK; v++) {
+        void* out = v == 0 ? ref.p : cur.p;
+        st_all = run(v, out);  // warm-up and the output to check
+        if (st_all != CY_OK) break;
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            st_all = set_error(CY_ERR_CUDA, "autotune warm-up failed");
+            break;
+        }
+        if (v > 0) {
+            cudaMemcpy(h_ref.data(), ref.p, out_bytes, cudaMemcpyDeviceToHost);
+            cudaMemcpy(h_cur.data(), cur.p, out_bytes, cudaMemcpyDeviceToHost);
+            if (std::memcmp(h_ref.data(), h_cur.data(), out_bytes) != 0) {
+                st_all = set_error(CY_ERR_INTERNAL, "autotune: a schedule disagrees with the default");
+                break;
+            }
+        }
+        const int reps = 3;
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps && st_all == CY_OK; r++) st_all = run(v, out);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (v == 0 || ms < best) {
+            best = ms;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st_all != CY_OK) return st_all;
+    set_choice(dev, logn, l64, op, best_v);
+    *chosen = best_v;
+    return CY_OK;
+}
+
+static cy_status tune_product(const Basis& B, bool centered, int batch, cudaStream_t st) {
+    const int n = B.h.n, l64 = B.h.l64;
+    const size_t bytes = sizeof(uint64_t) * (size_t)batch * n * l64;
+    std::vector<uint64_t> ha = random_polys(batch, n, l64, B.h.qbits, 1), hb = random_polys(batch, n, l64, B.h.qbits, 2);
+    DevBuf a, b;
+    CY_CUDA(cudaMalloc(&a.p, bytes));
+    CY_CUDA(cudaMalloc(&b.p, bytes));
+    CY_CUDA(cudaMemcpy(a.p, ha.data(), bytes, cudaMemcpyHostToDevice));
+    CY_CUDA(cudaMemcpy(b.p, hb.data(), bytes, cudaMemcpyHostToDevice));
+    Workspace ws;
+    CY_CUDA(cudaGetDevice(&ws.device));
+    const long long stride = (long long)n * l64;
+    const long long ostride = B.h.mode == EPI_DECRYPT ? n : stride;
+    const size_t obytes = sizeof(uint64_t) * (size_t)batch * ostride;
+    int chosen = 0;
+    return tune_op(B.h.logn, l64, centered ? TUNE_MULC : TUNE_MUL, obytes, st,
+                   [&](int v, void* out) {
+                       return run_product_api(B, centered, (const uint64_t*)a.p, stride, (const uint64_t*)b.p, stride,
+                                              out, ostride, batch, ws, st, v);
+                   },
+                   &chosen);
+}
+
+static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, int batch, cudaStream_t st) {
+    const int n = relin.h.n, l64 = relin.h.l64;
+    const size_t bytes = sizeof(uint64_t) * (size_t)batch * n * l64;
+    std::vector<uint64_t> hc = random_polys(batch, n, l64, relin.h.qbits, 3);
+    DevBuf c;
+    CY_CUDA(cudaMalloc(&c.p, bytes));
+    CY_CUDA(cudaMemcpy(c.p, hc.data(), bytes, cudaMemcpyHostToDevice));
+    Workspace ws;
+    CY_CUDA(cudaGetDevice(&ws.device));
+    int chosen = 0;
+    return tune_op(relin.h.logn, l64, TUNE_KS, bytes, st,
+                   [&](int v, void* out) {
+                       return run_keyswitch_api(relin, (const uint64_t*)c.p, evk, ell, (uint64_t*)out, batch, ws, st,
+                                                v);
+                   },
+                   &chosen);
+}
+
+}  // namespace cy
+
+using namespace cy;
+
+extern "C" {
+
+cy_status cy_ring_autotune(cy_ring* r, int batch, cy_stream_t stream) {
+    if (!r || batch < 1) return set_error(CY_ERR_INVALID_ARGUMENT, "bad argument");
+    std::lock_guard<std::mutex> lock(r->mu);
+    return tune_product(r->mul, false, batch, (cudaStream_t)stream);
+}
+
+cy_status cy_yashe_autotune(cy_yashe* y, int batch, cy_stream_t stream) {
+    if (!y || batch < 1) return set_error(CY_ERR_INVALID_ARGUMENT, "bad argument");
+    cy_ring* r = y->ring;
+    std::lock_guard<std::mutex> lock(r->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    CY_TRY(tune_product(r->mul, false, batch, st));
+    CY_TRY(tune_product(y->tensor, true, batch, st));
+    const uint2* evk = y->d_evk;
+    uint2* tmp = nullptr;
+    if (!evk) {  // no keys yet: an evaluation key of random values has the same cost
+        std::vector<uint64_t> h = random_polys(y->ell, r->n, r->l64, r->qbits, 4);
+        CY_TRY(prepare_evk(y->relin, h.data(), y->ell, r->n, r->l64, &tmp));
+        evk = tmp;
+    }
+    cy_status s = tune_keyswitch(y->relin, evk, y->ell, batch, st);
+    if (tmp) cudaFree(tmp);
+    return s;
+}
+
+cy_status cy_tuning_export(char* buf, size_t len, size_t* needed) {
+    int dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    std::ostringstream os;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        for (const auto& kv : g_choice) {
+            if (std::get<0>(kv.first) != dev) continue;
+            os << "n" << (1 << std::get<1>(kv.first)) << ".l" << std::get<2>(kv.first) << "."
+               << kOpNames[std::get<3>(kv.first)] << "=" << kv.second << ";";
+        }
+    }
+    const std::string s = os.str();
+    if (needed) *needed = s.size() + 1;
+    if (buf && len > 0) {
+        std::strncpy(buf, s.c_str(), len - 1);
+        buf[len - 1] = 0;
+        if (len < s.size() + 1) return set_error(CY_ERR_INVALID_ARGUMENT, "buffer too small");
+    }
+    return CY_OK;
+}
+
+cy_status cy_tuning_import(const char* spec) {
+    if (!spec) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL spec");
+    int dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    std::string s(spec);
+    size_t pos = 0;
+    while (pos < s.size()) {
+        size_t end = s.find(';', pos);
+        if (end == std::string::npos) end = s.size();
+        const std::string item = s.substr(pos, end - pos);
+        pos = end + 1;
+        if (item.empty()) continue;
+        int n = 0, l64 = 0, v = 0;
+        char op[8] = {0};
+        if (std::sscanf(item.c_str(), "n%d.l%d.%7[a-z]=%d", &n, &l64, op, &v) != 4)
+            return set_error(CY_ERR_INVALID_ARGUMENT, "bad tuning item: " + item);
+        int logn = 0;
+        while ((1 << logn) < n) logn++;
+        int o = -1;
+        for (int i = 0; i < TUNE_OPS; i++)
+            if (std::strcmp(op, kOpNames[i]) == 0) o = i;
+        if ((1 << logn) != n || logn < 1 || logn > LOGN_MAX || o < 0 || v < 0 || v >= variant_count(logn) ||
+            l64 < 1 || l64 > 6)
+            return set_error(CY_ERR_INVALID_ARGUMENT, "bad tuning item: " + item);
+        set_choice(dev, logn, l64, o, v);
+    }
+    return CY_OK;
+}
+
+}  // extern "C"

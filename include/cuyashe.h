@@ -230,6 +230,27 @@ cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, 
                        cy_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Schedule autotuning                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Each transform length is compiled with one or more NTT schedules (8 or 16
+ * coefficients per thread: 512 or 256 threads per transform and 4 or 3
+ * register passes at N = 4096). cy_ring_autotune runs every schedule of the
+ * ring's product on `batch` synthetic jobs, requires each output to equal the
+ * default schedule's bit for bit, and keeps the fastest for this device, N and
+ * limb count; cy_yashe_autotune does the same for the plain product, the YASHE
+ * tensor and the keyswitch. Synchronous; allocates its test buffers. The
+ * reference has one fixed launch shape per kernel (src/cuda_functions.cu:447-458)
+ * and hand-timed block sizes in comments (src/cuda_bn.cu:983-988). */
+cy_status cy_ring_autotune(cy_ring *ring, int batch, cy_stream_t stream);
+cy_status cy_yashe_autotune(cy_yashe *y, int batch, cy_stream_t stream);
+
+/* The current device's choices as text, e.g. "n4096.l2.mul=1;n4096.l2.ks=0;"
+ * (*needed gets the size including the terminator), and back. */
+cy_status cy_tuning_export(char *buf, size_t len, size_t *needed);
+cy_status cy_tuning_import(const char *spec);
+
+/* ------------------------------------------------------------------------ */
 /* Observability                                                              */
 /* ------------------------------------------------------------------------ */
 
