@@ -345,6 +345,61 @@ def run_ours(args):
         torch.cuda.synchronize()
     poly_plain = plain_calls / (time.perf_counter() - t0)
 
+    # ---- mixed batch: 512 products, N over {1024..8192}, q of 62/127/190 bits ---
+    mixed = None
+    try:
+        from cuyashe_gb300.api import polymul_batched, polymul_batched_status
+
+        mq = {62: 4611686018427322369, 127: Q_YASHE,
+              190: 1569275433846670190958947355801916604025588861116000698369}
+        rngm = np.random.default_rng(9)
+        specs = [(int(rngm.choice([1024, 2048, 4096, 8192])), int(rngm.choice([62, 127, 190]))) for _ in range(512)]
+        groups = {}
+        for (n_, b_) in specs:
+            groups.setdefault((n_, b_), 0)
+            groups[(n_, b_)] += 1
+        rings, bufs, jobs = {}, {}, []
+        for (n_, b_), cnt in groups.items():
+            Rm = cy.Ring(n_, mq[b_])
+            lm = Rm.L
+            hi_bits = (b_ - 1) - 64 * (lm - 1)  # values below 2^(b-1) < q
+            raw = rngm.integers(0, 2**63, size=(2, cnt, n_, lm), dtype=np.uint64)
+            raw[..., lm - 1] &= np.uint64((1 << hi_bits) - 1)
+            if lm > 1:
+                raw[..., :lm - 1] = rngm.integers(0, 2**64, size=(2, cnt, n_, lm - 1), dtype=np.uint64)
+            Am = torch.from_numpy(raw[0].view(np.int64)).cuda()
+            Bm = torch.from_numpy(raw[1].view(np.int64)).cuda()
+            Cm = Rm.empty(cnt)
+            rings[(n_, b_)], bufs[(n_, b_)] = Rm, (Am, Bm, Cm)
+            for j in range(cnt):
+                jobs.append((Rm, Am[j:j + 1], Bm[j:j + 1], Cm[j:j + 1]))
+        order = list(range(len(jobs)))
+        rngm.shuffle(order)
+        jobs = [jobs[i] for i in order]
+        polymul_batched(jobs)
+        polymul_batched_status()
+        ref = {key: bufs[key][2].clone() for key in bufs}
+
+        def grouped():
+            for key, Rm in rings.items():
+                Am, Bm, Cm = bufs[key]
+                Rm.polymul(Am, Bm, out=Cm)
+
+        grouped()
+        torch.cuda.synchronize()
+        same = all(torch.equal(ref[key], bufs[key][2]) for key in bufs)
+        msteps = max(5, args.steps // 4)
+        t_one = time_steps(lambda: polymul_batched(jobs), msteps, stream)
+        t_grp = time_steps(grouped, msteps, stream)
+        polymul_batched_status()
+        mixed = {"products": len(jobs), "classes": len(groups),
+                 "one_launch_products_per_s": len(jobs) * msteps / (t_one / 1000.0),
+                 "per_ring_products_per_s": len(jobs) * msteps / (t_grp / 1000.0),
+                 "one_launch_matches_per_ring": bool(same)}
+        log("mixed batch:", mixed)
+    except Exception as e:  # reported, not fatal for the headline
+        log("mixed batch failed:", e)
+
     # ---- e2e: host buffers, copies inside the timed region ----------------------
     H1 = C1.cpu().pin_memory()
     H2 = C2.cpu().pin_memory()
@@ -397,6 +452,7 @@ def run_ours(args):
         "plain_per_call": {"he_mults_per_s": plain_rate, "batched_over_plain": value / world / plain_rate},
         "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
                     "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
+        "mixed_batch": mixed,
         "decrypt_check": decrypt_ok,
         "cpu_baseline": cpu,
     }

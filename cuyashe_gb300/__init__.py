@@ -90,6 +90,7 @@ SIGNATURES = {
     "cy_poly_scalar_mul": ([_vp, _vp, _u64p, _vp, _i, _vp], _i),
     "cy_polymul_batched": ([ctypes.POINTER(PolymulJob), _i, _vp], _i),
     "cy_polymul_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_polymul_batched_status": ([_vp], _i),
     "cy_ntt": ([_vp, _vp, _i, _i, _vp], _i),
     "cy_crt": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_icrt": ([_vp, _vp, _vp, _i, _vp], _i),

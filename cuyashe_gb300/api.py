@@ -176,6 +176,11 @@ def polymul_batched(jobs: Sequence[tuple], stream=None) -> None:
     check(lib().cy_polymul_batched(arr, len(jobs), _stream_handle(stream)), "cy_polymul_batched")
 
 
+def polymul_batched_status(stream=None) -> None:
+    """Raise if a block of the last mixed launch gave up waiting (synchronises)."""
+    check(lib().cy_polymul_batched_status(_stream_handle(stream)), "cy_polymul_batched_status")
+
+
 class Yashe:
     """YASHE over Z_q[x]/(x^N+1) on the GPU (handle to a ``cy_yashe``)."""
 
@@ -265,5 +270,5 @@ class Yashe:
         return out
 
 
-__all__ = ["Ring", "Yashe", "Workspace", "polymul_batched", "to_limb_array", "from_limb_array", "to_device",
+__all__ = ["Ring", "Yashe", "Workspace", "polymul_batched", "polymul_batched_status", "to_limb_array", "from_limb_array", "to_device",
            "to_host", "nlimbs", "CY_OK"]

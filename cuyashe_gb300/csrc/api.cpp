@@ -15,6 +15,7 @@
 #include <mutex>
 #include <set>
 #include <utility>
+#include <vector>
 
 #include "host.h"
 
@@ -83,6 +84,9 @@ static cy_status check_device(int device) {
 }
 
 int tuned_variant(int logn, int l64, int op);
+cy_status run_mixed(const std::vector<const cy_polymul_job*>& jobs, cudaStream_t st);
+cy_status mixed_status(cudaStream_t st);
+bool mixed_supported(const cy_ring* r);
 
 // products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j); `variant`
 // selects the NTT schedule (-1: the tuned one for this device and size)
@@ -429,21 +433,29 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
 
 cy_status cy_polymul_batched(const cy_polymul_job* jobs, int njobs, cy_stream_t stream) {
     if (njobs < 0 || (njobs > 0 && !jobs)) return set_error(CY_ERR_INVALID_ARGUMENT, "bad job list");
-    // group consecutive jobs of the same ring whose buffers are contiguous
-    int i = 0;
-    while (i < njobs) {
-        cy_ring* r = jobs[i].ring;
-        CY_TRY(validate_poly_args(r, jobs[i].d_a, jobs[i].d_b, jobs[i].d_c, 1));
+    std::vector<const cy_polymul_job*> mixed, other;
+    for (int i = 0; i < njobs; i++) {
+        CY_TRY(validate_poly_args(jobs[i].ring, jobs[i].d_a, jobs[i].d_b, jobs[i].d_c, 1));
+        (mixed_supported(jobs[i].ring) ? mixed : other).push_back(&jobs[i]);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    CY_TRY(run_mixed(mixed, st));
+    // other rings: consecutive jobs of one ring with contiguous buffers share a launch
+    size_t i = 0;
+    while (i < other.size()) {
+        cy_ring* r = other[i]->ring;
         const long long stride = (long long)r->n * r->l64;
-        int j = i + 1;
-        while (j < njobs && jobs[j].ring == r && jobs[j].d_a == jobs[i].d_a + (j - i) * stride &&
-               jobs[j].d_b == jobs[i].d_b + (j - i) * stride && jobs[j].d_c == jobs[i].d_c + (j - i) * stride)
+        size_t j = i + 1;
+        while (j < other.size() && other[j]->ring == r && other[j]->d_a == other[i]->d_a + (j - i) * stride &&
+               other[j]->d_b == other[i]->d_b + (j - i) * stride && other[j]->d_c == other[i]->d_c + (j - i) * stride)
             j++;
-        CY_TRY(cy_polymul(r, jobs[i].d_a, jobs[i].d_b, jobs[i].d_c, j - i, stream));
+        CY_TRY(cy_polymul(r, other[i]->d_a, other[i]->d_b, other[i]->d_c, (int)(j - i), stream));
         i = j;
     }
     return CY_OK;
 }
+
+cy_status cy_polymul_batched_status(cy_stream_t stream) { return mixed_status((cudaStream_t)stream); }
 
 cy_status cy_ntt(cy_ring* r, uint32_t* d_res, int batch, int inverse, cy_stream_t stream) {
     CY_TRY(validate_poly_args(r, d_res, d_res, d_res, batch));

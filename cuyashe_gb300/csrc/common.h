@@ -51,4 +51,22 @@ struct BasisDev {
     const uint2* ipsi[KMAX];    // inverse twiddles
 };
 
+// One product of a mixed batch (different N and q per job) for the persistent
+// kernel k_mixed.
+struct MixedJob {
+    const BasisDev* B;  // the job's product basis (mod-q epilogue)
+    const uint64_t* a;
+    const uint64_t* b;
+    uint64_t* c;
+    uint32_t* resid;    // [k][N] residues of this job in the batch scratch
+    int logn, k, l32, l64;
+};
+
+// A unit of work claimed by one block: kind 0 runs the NTT product of `count`
+// consecutive primes of a job starting at `first`; kind 1 runs the ICRT
+// epilogue of coefficients [first, first + count) once all primes are done.
+struct MixedUnit {
+    int job, kind, first, count;
+};
+
 }  // namespace cy

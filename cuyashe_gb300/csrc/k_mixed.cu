@@ -1,0 +1,124 @@
+// k_mixed: one persistent launch for a batch of products of different rings
+// (N from 1024 to 8192, q up to 192 bits): the fused CRT -> NTT -> pointwise ->
+// INTT -> ICRT -> mod q path over a work list.
+//
+// Blocks of 512 threads claim units from an atomic counter. The NTT units come
+// first, largest transforms first; a unit of N = 2048 or 1024 runs 2 or 4 primes
+// of its job side by side, each on its own named barrier. The epilogue units of
+// a job follow all NTT units; a block that claims one waits until every prime of
+// that job is done. Those primes were claimed earlier by running blocks that
+// never wait, so the wait ends; the spin is still bounded, and on expiry the
+// block records an error word and skips the unit instead of hanging.
+#include "kernels.cuh"
+
+namespace cy {
+
+constexpr int kMixedThreads = 512;
+constexpr unsigned kMixedSpinLimit = 1u << 24;  // ~ seconds with the back-off below
+
+template <int LOGN, int LOGE>
+__device__ __forceinline__ void mixed_ntt_unit(const MixedJob& J, const MixedUnit& U, uint32_t* smem,
+                                               uint32_t* __restrict__ done) {
+    using PL = NttPlan<LOGN, LOGE>;
+    constexpr int E = PL::E, G = PL::G;
+    constexpr int NSUB = kMixedThreads / G;
+    // exchange regions of one sub-group: double-buffered below 8192, single above
+    constexpr int SUBW = (NSUB > 1 || LOGN < 13) ? 4 * PL::SMW : 2 * PL::SMW;
+    constexpr int STRIDE = (NSUB > 1 || LOGN < 13) ? 2 * PL::SMW : 0;
+    const int sub = threadIdx.x / G, tau = threadIdx.x % G;
+    if (sub >= U.count) return;  // fewer primes than sub-groups in this unit
+    const int prime = U.first + sub;
+    const GroupSync bar{1 + sub, G};
+    uint32_t* sm = smem + sub * SUBW;
+    const BasisDev* __restrict__ B = J.B;
+    const PrimeCtx c = load_prime_ctx(B, prime);
+    const uint32_t* crt = B->crt[prime];
+    uint32_t x[2][E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int pos = slot_pos<PL, 0>(tau, e);
+        x[0][e] = crt_coef<false>(J.a, pos, J.l64, crt, nullptr, c);
+        x[1][e] = crt_coef<false>(J.b, pos, J.l64, crt, nullptr, c);
+    }
+    int buf = ntt_forward<PL, 2, GroupSync>(x, B->psi[prime], c.p, tau, sm, STRIDE, 0, bar);
+    uint32_t z[1][E];
+#pragma unroll
+    for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
+    ntt_inverse<PL, 1, GroupSync>(z, B->ipsi[prime], c.p, tau, sm, STRIDE, buf, bar);
+    uint32_t* out = J.resid + (size_t)prime * PL::N;
+#pragma unroll
+    for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];
+    __threadfence();  // residues visible device-wide before the count says so
+    bar.sync();
+    if (tau == 0) atomicAdd(&done[U.job], 1u);
+}
+
+template <int L>
+__device__ __forceinline__ void mixed_epi_coefs(const MixedJob& J, const MixedUnit& U, EpiShared& S) {
+    epi_stage<L, EPI_MODQ>(S, J.B, threadIdx.x, kMixedThreads);
+    __syncthreads();
+    const size_t n = (size_t)1 << J.logn;
+    for (int coef = U.first + threadIdx.x; coef < U.first + U.count; coef += kMixedThreads)
+        epi_coef<L, EPI_MODQ>(S, J.B, J.resid + coef, n, J.c + (size_t)coef * J.l64);
+}
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(kMixedThreads, 2)
+    k_mixed(const MixedJob* __restrict__ jobs, const MixedUnit* __restrict__ units, int n_units,
+            uint32_t* __restrict__ done, uint32_t* __restrict__ ctl) {
+    extern __shared__ uint32_t smem[];
+    __shared__ EpiShared S;
+    __shared__ int s_unit, s_ok;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = (int)atomicAdd(&ctl[0], 1u);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= n_units) break;
+        const MixedUnit U = units[u];
+        const MixedJob J = jobs[U.job];
+        if (U.kind == 0) {
+            switch (J.logn) {
+                case 10: mixed_ntt_unit<10, 3>(J, U, smem, done); break;
+                case 11: mixed_ntt_unit<11, 3>(J, U, smem, done); break;
+                case 12: mixed_ntt_unit<12, 3>(J, U, smem, done); break;
+                case 13: mixed_ntt_unit<13, 4>(J, U, smem, done); break;
+                default: break;
+            }
+        } else {
+            if (threadIdx.x == 0) {
+                unsigned spins = 0;
+                while (load_acquire(&done[U.job]) < (uint32_t)J.k && spins < kMixedSpinLimit) {
+                    __nanosleep(256);
+                    spins++;
+                }
+                s_ok = spins < kMixedSpinLimit;
+                if (!s_ok) atomicExch(&ctl[1], 1u);
+            }
+            __syncthreads();
+            if (s_ok) {
+                __threadfence();
+                switch (J.l32) {
+                    case 1: mixed_epi_coefs<1>(J, U, S); break;
+                    case 2: mixed_epi_coefs<2>(J, U, S); break;
+                    case 3: mixed_epi_coefs<3>(J, U, S); break;
+                    case 4: mixed_epi_coefs<4>(J, U, S); break;
+                    case 5: mixed_epi_coefs<5>(J, U, S); break;
+                    case 6: mixed_epi_coefs<6>(J, U, S); break;
+                    default: break;
+                }
+            }
+        }
+        __syncthreads();  // shared memory and s_unit are reused by the next unit
+    }
+}
+
+void* mixed_kernel() { return (void*)k_mixed; }
+size_t mixed_smem_bytes() { return (size_t)4 * NttPlan<12, 3>::SMW * sizeof(uint32_t); }
+int mixed_threads() { return kMixedThreads; }
+
+}  // namespace cy

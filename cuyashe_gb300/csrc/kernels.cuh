@@ -439,37 +439,38 @@ struct EpiShared {
     uint32_t B0[L32MAX], B1[L32MAX], qn[L32MAX], qhalf_n[L32MAX];
 };
 
+// Copy the epilogue constants of basis B into shared memory (threads tid, tid +
+// nthreads, ... of the caller's group).
 template <int L, int MODE>
-__global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
-                                             void* __restrict__ out, int njobs) {
-    __shared__ EpiShared S;
-    const int k = B->k, logn = B->logn, shift = B->shift, l64 = B->l64;
-    const uint64_t mu = B->mu;
-    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+__device__ __forceinline__ void epi_stage(EpiShared& S, const BasisDev* __restrict__ B, int tid, int nthreads) {
+    const int k = B->k;
+    for (int i = tid; i < k; i += nthreads) {
         S.p[i] = B->p[i];
         S.ycon[i] = B->ycon[i];
         S.ycon_sh[i] = B->ycon_sh[i];
         S.flo[i] = B->flo[i];
         S.fhi[i] = B->fhi[i];
     }
-    for (int i = threadIdx.x; i < k * L; i += blockDim.x) {
+    for (int i = tid; i < k * L; i += nthreads) {
         S.A0[i] = B->A0[i / L][i % L];
         if (MODE == EPI_YASHE) S.A1[i] = B->A1[i / L][i % L];
     }
-    if (threadIdx.x < L) {
-        S.B0[threadIdx.x] = B->B0[threadIdx.x];
-        S.B1[threadIdx.x] = B->B1[threadIdx.x];
-        S.qn[threadIdx.x] = B->qn[threadIdx.x];
-        S.qhalf_n[threadIdx.x] = B->qhalf_n[threadIdx.x];
+    for (int i = tid; i < L; i += nthreads) {
+        S.B0[i] = B->B0[i];
+        S.B1[i] = B->B1[i];
+        S.qn[i] = B->qn[i];
+        S.qhalf_n[i] = B->qhalf_n[i];
     }
-    __syncthreads();
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = 1 << logn;
-    const long long job = idx >> logn;
-    if (job >= njobs) return;
-    const int coef = (int)(idx & (n - 1));
-    const uint32_t* r0 = resid + (size_t)job * k * n + coef;
+}
 
+// Epilogue of one coefficient: r0 points at its residue for prime 0, residues of
+// the next primes follow `stride` words apart. Writes limb j of `dst` (MODQ,
+// YASHE) or one word (DECRYPT).
+template <int L, int MODE>
+__device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __restrict__ B,
+                                         const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst) {
+    const int k = B->k, shift = B->shift, l64 = B->l64;
+    const uint64_t mu = B->mu;
     Cols<L> c0, c1;
     c0.zero();
     c1.zero();
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
     constexpr int KU = 15;
     uint32_t rk[KU];
 #pragma unroll
-    for (int i = 0; i < KU; i++) rk[i] = (i < k) ? __ldcg(r0 + (size_t)i * n) : 0u;
+    for (int i = 0; i < KU; i++) rk[i] = (i < k) ? __ldcg(r0 + (size_t)i * stride) : 0u;
 #pragma unroll
     for (int i = 0; i < KU; i++) {
         if (i < k) absorb(i, rk[i]);
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
     for (int i0 = KU; i0 < k; i0 += 3) {  // bases of more than KU primes
         uint32_t rr[3];
 #pragma unroll
-        for (int j = 0; j < 3; j++) rr[j] = (i0 + j < k) ? __ldcg(r0 + (size_t)(i0 + j) * n) : 0u;
+        for (int j = 0; j < 3; j++) rr[j] = (i0 + j < k) ? __ldcg(r0 + (size_t)(i0 + j) * stride) : 0u;
 #pragma unroll
         for (int j = 0; j < 3; j++)
             if (i0 + j < k) absorb(i0 + j, rr[j]);
@@ -536,7 +537,7 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
         uint32_t rd[L];
         uint64_t Q = barrett<L>(c2, S.qn, mu, rd);  // round(t x / q) in [0, t]
         if (Q >= B->t) Q -= B->t;
-        reinterpret_cast<uint64_t*>(out)[job * n + coef] = Q;
+        dst[0] = Q;
     } else {
         uint32_t o[L];
 #pragma unroll
@@ -544,14 +545,30 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
             const uint32_t nx = (w + 1 < L) ? r[w + 1] : 0u;
             o[w] = __funnelshift_r(r[w], nx, shift);
         }
-        uint64_t* dst = reinterpret_cast<uint64_t*>(out) + ((size_t)job * n + coef) * l64;
 #pragma unroll
         for (int j = 0; j < (L + 1) / 2; j++) {
             const uint64_t lo32 = o[2 * j];
             const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
-            dst[j] = lo32 | (hi32 << 32);
+            if (j < l64) dst[j] = lo32 | (hi32 << 32);
         }
     }
+}
+
+template <int L, int MODE>
+__global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
+                                             void* __restrict__ out, int njobs) {
+    __shared__ EpiShared S;
+    epi_stage<L, MODE>(S, B, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int logn = B->logn, k = B->k, l64 = B->l64;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = 1 << logn;
+    const long long job = idx >> logn;
+    if (job >= njobs) return;
+    const int coef = (int)(idx & (n - 1));
+    uint64_t* dst = reinterpret_cast<uint64_t*>(out) +
+                    (MODE == EPI_DECRYPT ? (size_t)job * n + coef : ((size_t)job * n + coef) * l64);
+    epi_coef<L, MODE>(S, B, resid + (size_t)job * k * n + coef, (size_t)n, dst);
 }
 
 }  // namespace cy

@@ -45,6 +45,19 @@ struct NttPlan {
     __host__ __device__ static constexpr int LOGD(int pass) { return LOGN - S0(pass) - R(pass); }
 };
 
+// Barrier of the threads that own one transform: the whole block, or a named
+// barrier (ids 1..15) shared by `count` threads when a block runs several
+// independent transforms side by side.
+struct CtaSync {
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+struct GroupSync {
+    int id, count;
+    __device__ __forceinline__ void sync() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    }
+};
+
 // one padding word per 32: position -> shared-memory word
 __device__ __forceinline__ int padi(int pos) { return pos + (pos >> 5); }
 __host__ __device__ constexpr int padc(int c) { return c + (c >> 5); }
@@ -127,11 +140,12 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 // between two such regions need one barrier (the next write cannot race with a
 // slow reader of this region); a caller with a single region passes
 // `sync_before` to add a barrier ahead of the writes.
-template <class PL, int PA, int PB, int NOPS>
-__device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* sm, int tau, bool sync_before) {
+template <class PL, int PA, int PB, int NOPS, class Sync = CtaSync>
+__device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* sm, int tau, bool sync_before,
+                                         Sync bar = Sync()) {
     constexpr int RA = PL::R(PA), LA = PL::LOGD(PA), NVA = PL::E >> RA;
     constexpr int RB = PL::R(PB), LB = PL::LOGD(PB), NVB = PL::E >> RB;
-    if (sync_before) __syncthreads();
+    if (sync_before) bar.sync();
 #pragma unroll
     for (int v = 0; v < NVA; v++) {
         const int base = padi(group_base<PL, PA>(tau, v));
@@ -141,7 +155,7 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* s
             for (int o = 0; o < NOPS; o++) sm[o * PL::SMW + base + padc(u << LA)] = x[o][(v << RA) + u];
         }
     }
-    __syncthreads();
+    bar.sync();
 #pragma unroll
     for (int v = 0; v < NVB; v++) {
         const int base = padi(group_base<PL, PB>(tau, v));
@@ -157,50 +171,52 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* s
 // block; exchange number b uses region (b & 1) of `sm`, regions `stride` words
 // apart (stride >= NOPS * SMW for every NOPS the kernel uses), or the single
 // region `sm` when stride == 0. Returns the updated count.
-template <class PL, int PASS, int NOPS>
+template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct FwdFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
-                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf) {
+                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf,
+                                              Sync bar = Sync()) {
         if constexpr (PASS >= PL::NPASS) {
             return buf;
         } else {
-            exchange<PL, PASS - 1, PASS, NOPS>(x, sm + (buf & 1) * stride, tau, stride == 0);
+            exchange<PL, PASS - 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
             fwd_pass<PL, PASS, NOPS>(x, tw, p, tau);
-            return FwdFrom<PL, PASS + 1, NOPS>::run(x, tw, p, tau, sm, stride, buf + 1);
+            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar);
         }
     }
 };
 
 // Inverse passes PASS .. 0 where pass PASS+1 was the previous one.
-template <class PL, int PASS, int NOPS>
+template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct InvFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
-                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf) {
+                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf,
+                                              Sync bar = Sync()) {
         if constexpr (PASS < 0) {
             return buf;
         } else {
-            exchange<PL, PASS + 1, PASS, NOPS>(x, sm + (buf & 1) * stride, tau, stride == 0);
+            exchange<PL, PASS + 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
             inv_pass<PL, PASS, NOPS>(x, tw, p, tau);
-            return InvFrom<PL, PASS - 1, NOPS>::run(x, tw, p, tau, sm, stride, buf + 1);
+            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar);
         }
     }
 };
 
 // Full forward transform: registers in pass-0 layout (natural order) ->
 // registers in last-pass layout (bit-reversed order).
-template <class PL, int NOPS>
+template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                           int tau, uint32_t* sm, int stride, int buf) {
+                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync()) {
     fwd_pass<PL, 0, NOPS>(x, tw, p, tau);
-    return FwdFrom<PL, 1, NOPS>::run(x, tw, p, tau, sm, stride, buf);
+    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar);
 }
 
 // Full inverse transform: registers in last-pass layout -> pass-0 layout.
-template <class PL, int NOPS>
+template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                           int tau, uint32_t* sm, int stride, int buf) {
+                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync()) {
     inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau);
-    return InvFrom<PL, PL::NPASS - 2, NOPS>::run(x, tw, p, tau, sm, stride, buf);
+    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar);
 }
 
 }  // namespace cy

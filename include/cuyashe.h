@@ -139,8 +139,15 @@ cy_status cy_poly_scalar_mul(cy_ring *ring, const uint64_t *d_a, const uint64_t 
 cy_status cy_polymul_noalloc(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
                              cy_stream_t stream);
 
-/* Mixed batch: products of different rings (different N and q) in one
- * submission. Jobs are grouped by ring and launched back to back on `stream`. */
+/* Mixed batch: `njobs` products, each of its own ring (N and q may differ per
+ * job). Products of rings with N in 1024..8192 and q up to 192 bits run in ONE
+ * persistent launch that fuses CRT, forward NTTs, pointwise product, inverse
+ * NTT, ICRT and mod q over a work list (largest transforms first, epilogue
+ * units after the NTT units of their job); products of other rings go through
+ * the per-ring path in the same call. The reference multiplies one pair per
+ * call and re-initialises its tables whenever N changes (src/common.h:136-226).
+ * Asynchronous on `stream`; calls on different streams are ordered on the
+ * device by the library (they share one scratch per device). */
 typedef struct cy_polymul_job {
     cy_ring *ring;
     const uint64_t *d_a;
@@ -148,6 +155,11 @@ typedef struct cy_polymul_job {
     uint64_t *d_c;
 } cy_polymul_job;
 cy_status cy_polymul_batched(const cy_polymul_job *jobs, int njobs, cy_stream_t stream);
+
+/* Synchronises `stream` with the last mixed launch on this device and reports
+ * CY_ERR_TIMEOUT if a block of it gave up waiting for its job's transforms (a
+ * bounded wait that cannot expire unless the device stops making progress). */
+cy_status cy_polymul_batched_status(cy_stream_t stream);
 
 /* Forward / inverse negacyclic NTT of residue vectors: d_res is [batch][k][N]
  * uint32 residues modulo the ring's CRT primes, transformed in place (values

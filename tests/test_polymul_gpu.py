@@ -269,3 +269,44 @@ def test_batched_mixed_rings_same_as_alone(cy):
         got = R.download(C)
         for j in range(3):
             assert list(got[j]) == ring.polymul_mod(a[j], b[j], q)
+
+
+def test_mixed_batch_one_launch_config3(cy):
+    """512 products, N uniform over {1024, 2048, 4096, 8192}, q of 62/127/190 bits:
+    one persistent launch; every product equals the per-ring result, a sample
+    equals the oracle; rings outside the mixed kernel's range (N = 16384, a
+    380-bit q) ride along in the same submission."""
+    import torch
+
+    from cuyashe_gb300.api import polymul_batched, polymul_batched_status
+
+    rng = random.Random(512)
+    qs = [Q62, Q127, Q190]
+    ns = [1024, 2048, 4096, 8192]
+    rings = {(n, q): cy.Ring(n, q) for n in ns for q in qs}
+    rings[(16384, Q62)] = cy.Ring(16384, Q62)
+    rings[(1024, Q380)] = cy.Ring(1024, Q380)
+    specs = [(rng.choice(ns), rng.choice(qs)) for _ in range(512)] + [(16384, Q62), (1024, Q380)]
+    jobs, data = [], []
+    for n, q in specs:
+        R = rings[(n, q)]
+        a = [rng.randrange(q) for _ in range(n)]
+        b = [rng.randrange(q) for _ in range(n)]
+        A, B = R.upload([a]), R.upload([b])
+        C = R.empty(1)
+        jobs.append((R, A, B, C))
+        data.append((a, b, q))
+    polymul_batched(jobs)
+    polymul_batched_status()
+    torch.cuda.synchronize()
+    for (R, A, B, C) in jobs:
+        assert torch.equal(R.polymul(A, B), C)
+    for idx in [0, 1, 7, 100, 255, 511, 512, 513]:
+        R, A, B, C = jobs[idx]
+        a, b, q = data[idx]
+        assert list(R.download(C)[0]) == ring.polymul_mod(a, b, q)
+    # a second submission on the same scratch
+    polymul_batched(jobs[:64])
+    polymul_batched_status()
+    for (R, A, B, C) in jobs[:64]:
+        assert torch.equal(R.polymul(A, B), C)
