@@ -165,6 +165,122 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------
+# serving (Poisson arrivals of mixed-size HE multiplies)
+# ----------------------------------------------------------------------------
+
+SERVE_CLASSES = [  # (N, q, t, weight): q = largest prime below 2^b with q = 1 (mod 2^16)
+    (2048, 4611686018427322369, 257, 0.4),
+    (4096, Q_YASHE, 1024, 0.3),
+    (8192, 1569275433846670190958947355801916604025588861116000698369, 65537, 0.2),
+    (16384, None, 65537, 0.1),
+]
+
+
+def _q380():
+    # largest prime below 2^380 with q = 1 (mod 2^16); primality by Miller-Rabin
+    def is_prime(n):
+        d, r = n - 1, 0
+        while d % 2 == 0:
+            d //= 2
+            r += 1
+        for a in (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37):
+            x = pow(a, d, n)
+            if x in (1, n - 1):
+                continue
+            for _ in range(r - 1):
+                x = x * x % n
+                if x == n - 1:
+                    break
+            else:
+                return False
+        return True
+    p = ((2**380 - 2) >> 16 << 16) + 1
+    while not is_prime(p):
+        p -= 1 << 16
+    return p
+
+
+def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2024):
+    import numpy as np
+    import torch
+
+    from cuyashe_gb300.api import Server, Yashe
+
+    classes = []
+    for n, q, t, w in SERVE_CLASSES:
+        q = q or _q380()
+        y = Yashe(n, q, t)
+        y.keygen(n + 17)
+        pool = 8
+        rng = np.random.default_rng(n)
+        m = rng.integers(0, t, size=(2 * pool, n), dtype=np.uint64)
+        ct = y.encrypt_host(m, seed=n)
+        classes.append({"y": y, "w": w, "ct": ct, "pool": pool, "n": n, "qbits": q.bit_length()})
+    rng = np.random.default_rng(seed)
+    count = int(rate_per_s * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
+    weights = np.array([c["w"] for c in classes])
+    kinds = rng.choice(len(classes), size=count, p=weights / weights.sum())
+    picks = rng.integers(0, 8, size=(count, 2))
+    outs = [np.zeros((256,) + c["ct"].shape[1:], np.uint64) for c in classes]  # reused cyclically
+
+    srv = Server(budget_bytes=120 << 30, streams=4, max_batch=256)
+    ids = [srv.register(c["y"]) for c in classes]
+    # warm-up: one batch per class
+    warm = [srv.submit(ids[k], c["ct"][0], c["ct"][1], outs[k][0]) for k, c in enumerate(classes)]
+    for t in warm:
+        srv.wait(t)
+    srv.reset_stats()
+    tickets = []
+    t0 = time.perf_counter()
+    for i in range(count):
+        while time.perf_counter() - t0 < arrivals[i]:
+            pass
+        k = int(kinds[i])
+        c = classes[k]
+        tickets.append(srv.submit(ids[k], c["ct"][picks[i, 0]], c["ct"][c["pool"] + picks[i, 1]],
+                                  outs[k][i % 256]))
+    srv.drain()
+    for t in tickets:
+        srv.wait(t)
+    st = srv.stats()
+    served = {"requests": count, "offered_rate_per_s": rate_per_s, "throughput_per_s": st.throughput_per_s,
+              "p50_ms": st.p50_us / 1000.0, "p99_ms": st.p99_us / 1000.0, "mean_ms": st.mean_us / 1000.0,
+              "batches": int(st.batches), "failed": int(st.failed), "peak_device_gb": st.peak_device_bytes / 1e9,
+              "mix": {"%d/%d" % (c["n"], c["qbits"]): c["w"] for c in classes}}
+    srv.close()
+
+    # the plain per-request path on the same trace prefix: one multiply per
+    # request, in arrival order, host buffers copied in and out each time
+    lat = []
+    stream = torch.cuda.current_stream()
+    dev = {}
+    for k, c in enumerate(classes):
+        shp = c["ct"].shape[1:]
+        dev[k] = (torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
+                  torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
+                  torch.empty((1,) + shp, dtype=torch.int64, device="cuda"))
+    pinned = {k: torch.from_numpy(c["ct"].view(np.int64)).pin_memory() for k, c in enumerate(classes)}
+    t0 = time.perf_counter()
+    for i in range(min(plain_prefix, count)):
+        while time.perf_counter() - t0 < arrivals[i]:
+            pass
+        k = int(kinds[i])
+        c = classes[k]
+        d1, d2, do = dev[k]
+        d1[0].copy_(pinned[k][picks[i, 0]], non_blocking=True)
+        d2[0].copy_(pinned[k][c["pool"] + picks[i, 1]], non_blocking=True)
+        c["y"].mul(d1, d2, relin=True, out=do)
+        do.cpu()
+        lat.append(time.perf_counter() - t0 - arrivals[i])
+    span = time.perf_counter() - t0
+    lat = np.array(lat) * 1000.0
+    plain = {"requests": len(lat), "throughput_per_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
+             "p99_ms": float(np.percentile(lat, 99))}
+    return {"continuous_batching": served, "plain_per_request": plain}
+
+
+# ----------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------
 
@@ -324,6 +440,26 @@ def run_ours(args):
     plain()
     plain_rate = plain_calls / (time.perf_counter() - t0)
 
+    # ---- CUDA graphs: the batched step and a one-pair call, replayed ----------
+    graphs = None
+    try:
+        g_step = Y.mul_graph(C1, C2, OUT, relin=True)
+        g_step.launch()
+        torch.cuda.synchronize()
+        g_ms = time_steps(lambda: g_step.launch(stream), args.steps, stream)
+        g_one = Y.mul_graph(C1[:1], C2[:1], o1, relin=True)
+        g_one.launch()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j in range(plain_calls):
+            g_one.launch(stream)
+            torch.cuda.synchronize()
+        graphs = {"batched_he_mults_per_s": B * args.steps / (g_ms / 1000.0),
+                  "per_call_he_mults_per_s": plain_calls / (time.perf_counter() - t0)}
+        del g_step, g_one
+    except Exception as e:
+        log("graph replay failed:", e)
+
     # ---- polynomial products (Polynomial c = a*b; c.reduce()) ------------------
     R = cy.Ring(N, Q_POLY)
     if not args.no_autotune:
@@ -400,6 +536,15 @@ def run_ours(args):
     except Exception as e:  # reported, not fatal for the headline
         log("mixed batch failed:", e)
 
+    # ---- serving: Poisson arrivals of mixed-size multiplies --------------------
+    serving = None
+    if not args.no_serving:
+        try:
+            serving = serving_bench(cy)
+            log("serving:", serving)
+        except Exception as e:
+            log("serving bench failed:", e)
+
     # ---- e2e: host buffers, copies inside the timed region ----------------------
     H1 = C1.cpu().pin_memory()
     H2 = C2.cpu().pin_memory()
@@ -453,6 +598,8 @@ def run_ours(args):
         "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
                     "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
         "mixed_batch": mixed,
+        "cuda_graph": graphs,
+        "serving": serving,
         "decrypt_check": decrypt_ok,
         "cpu_baseline": cpu,
     }
@@ -470,6 +617,9 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="ciphertext pairs per GPU per step")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT schedules")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serving-only", type=float, default=0.0, metavar="SECONDS",
+                    help="run only the serving measurement over SECONDS of arrivals and print it")
     ap.add_argument("--ncu-step", action="store_true",
                     help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
     args = ap.parse_args()
@@ -478,6 +628,11 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.serving_only > 0:
+        import cuyashe_gb300 as cy
+
+        cy.lib()
+        print(json.dumps(serving_bench(cy, seconds=args.serving_only)), flush=True)
     else:
         run_ours(args)
 

@@ -63,6 +63,23 @@ class TraceEntry(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device_budget_bytes", ctypes.c_size_t), ("streams", ctypes.c_int), ("max_batch", ctypes.c_int),
+                ("poll_us", ctypes.c_int)]
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("class_id", ctypes.c_int), ("relin", ctypes.c_int), ("h_c1", ctypes.c_void_p),
+                ("h_c2", ctypes.c_void_p), ("h_out", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
+                ("mean_us", ctypes.c_double), ("throughput_per_s", ctypes.c_double),
+                ("peak_device_bytes", ctypes.c_size_t)]
+
+
 class PolymulJob(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_void_p), ("d_a", ctypes.c_void_p), ("d_b", ctypes.c_void_p),
                 ("d_c", ctypes.c_void_p)]
@@ -107,6 +124,19 @@ SIGNATURES = {
     "cy_yashe_mul_ws": ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)], _i),
+    "cy_server_destroy": ([_vp], _i),
+    "cy_server_register": ([_vp, _vp, ctypes.POINTER(_i)], _i),
+    "cy_server_submit": ([_vp, ctypes.POINTER(ServeRequest), ctypes.POINTER(ctypes.c_uint64)], _i),
+    "cy_server_poll": ([_vp, ctypes.c_uint64, ctypes.POINTER(_i)], _i),
+    "cy_server_wait": ([_vp, ctypes.c_uint64, _i], _i),
+    "cy_server_drain": ([_vp, _i], _i),
+    "cy_server_get_stats": ([_vp, ctypes.POINTER(ServerStats)], _i),
+    "cy_server_reset_stats": ([_vp], _i),
+    "cy_polymul_graph_create": ([_vp, _vp, _vp, _vp, _i, ctypes.POINTER(_vp)], _i),
+    "cy_yashe_mul_graph_create": ([_vp, _vp, _vp, _vp, _i, _i, ctypes.POINTER(_vp)], _i),
+    "cy_graph_launch": ([_vp, _vp], _i),
+    "cy_graph_destroy": ([_vp], _i),
     "cy_ring_autotune": ([_vp, _i, _vp], _i),
     "cy_yashe_autotune": ([_vp, _i, _vp], _i),
     "cy_tuning_export": ([ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], _i),

@@ -19,8 +19,8 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from . import (CY_OK, PolymulJob, RingInfo, YasheInfo, YasheParams, _ptr, _stream_handle, check, lib,
-               limbs_of)
+from . import (CY_OK, PolymulJob, RingInfo, ServeRequest, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
+               _stream_handle, check, lib, limbs_of)
 
 
 def nlimbs(q: int) -> int:
@@ -66,6 +66,22 @@ class Workspace:
         if getattr(self, "h", None) and self.h.value:
             lib().cy_workspace_destroy(self.h)
             self.h = None
+
+
+class Graph:
+    """A fixed batch recorded as a CUDA graph (``cy_*_graph_create``); keeps its
+    buffers alive and replays with ``launch``."""
+
+    def __init__(self, handle: ctypes.c_void_p, keep):
+        self.h, self._keep = handle, keep
+
+    def launch(self, stream=None) -> None:
+        check(lib().cy_graph_launch(self.h, _stream_handle(stream)), "cy_graph_launch")
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().cy_graph_destroy(self.h)
+            self.h = ctypes.c_void_p()
 
 
 class Ring:
@@ -145,6 +161,12 @@ class Ring:
 
     def autotune(self, batch: int = 256, stream=None) -> None:
         check(lib().cy_ring_autotune(self.h, batch, _stream_handle(stream)), "cy_ring_autotune")
+
+    def polymul_graph(self, a, b, out) -> Graph:
+        h = ctypes.c_void_p()
+        check(lib().cy_polymul_graph_create(self.h, _ptr(a), _ptr(b), _ptr(out), a.shape[0], ctypes.byref(h)),
+              "cy_polymul_graph_create")
+        return Graph(h, (a, b, out))
 
     def residues_empty(self, batch: int):
         import torch
@@ -257,6 +279,12 @@ class Yashe:
                                         1 if relin else 0, st), "cy_yashe_mul_ws")
         return out
 
+    def mul_graph(self, c1, c2, out, relin: bool = True) -> Graph:
+        h = ctypes.c_void_p()
+        check(lib().cy_yashe_mul_graph_create(self.h, _ptr(c1), _ptr(c2), _ptr(out), c1.shape[0], 1 if relin else 0,
+                                              ctypes.byref(h)), "cy_yashe_mul_graph_create")
+        return Graph(h, (c1, c2, out, self))
+
     def keyswitch(self, c, out=None, stream=None):
         out = self.ring.empty(c.shape[0]) if out is None else out
         check(lib().cy_yashe_keyswitch(self.h, _ptr(c), _ptr(out), c.shape[0], _stream_handle(stream)),
@@ -270,5 +298,73 @@ class Yashe:
         return out
 
 
-__all__ = ["Ring", "Yashe", "Workspace", "polymul_batched", "polymul_batched_status", "to_limb_array", "from_limb_array", "to_device",
+class Server:
+    """Continuous-batching request loop (``cy_server``) for YASHE multiplies.
+
+    Requests carry host numpy arrays [N][L] (uint64); the server keeps references
+    to them until ``wait`` returns for the ticket.
+    """
+
+    def __init__(self, budget_bytes: int, streams: int = 4, max_batch: int = 256, poll_us: int = 20):
+        cfg = ServerConfig(device_budget_bytes=budget_bytes, streams=streams, max_batch=max_batch, poll_us=poll_us)
+        h = ctypes.c_void_p()
+        check(lib().cy_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cy_server_create")
+        self.h = h
+        self._keep = {}
+        self._contexts = []
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().cy_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+        self._keep.clear()
+
+    def __del__(self):
+        self.close()
+
+    def register(self, y: "Yashe") -> int:
+        cid = ctypes.c_int(0)
+        check(lib().cy_server_register(self.h, y.h, ctypes.byref(cid)), "cy_server_register")
+        self._contexts.append(y)
+        return cid.value
+
+    def submit(self, class_id: int, c1: np.ndarray, c2: np.ndarray, out: np.ndarray, relin: bool = True) -> int:
+        req = ServeRequest(class_id=class_id, relin=1 if relin else 0, h_c1=c1.ctypes.data, h_c2=c2.ctypes.data,
+                           h_out=out.ctypes.data)
+        t = ctypes.c_uint64(0)
+        check(lib().cy_server_submit(self.h, ctypes.byref(req), ctypes.byref(t)), "cy_server_submit")
+        self._keep[t.value] = (c1, c2, out)
+        return t.value
+
+    def submit_status(self, class_id: int, c1, c2, out, relin: bool = True) -> int:
+        """cy_server_submit's raw status (for rejection tests)."""
+        req = ServeRequest(class_id=class_id, relin=1 if relin else 0, h_c1=c1.ctypes.data if c1 is not None else 0,
+                           h_c2=c2.ctypes.data if c2 is not None else 0, h_out=out.ctypes.data if out is not None else 0)
+        t = ctypes.c_uint64(0)
+        return lib().cy_server_submit(self.h, ctypes.byref(req), ctypes.byref(t))
+
+    def poll(self, ticket: int) -> bool:
+        d = ctypes.c_int(0)
+        check(lib().cy_server_poll(self.h, ticket, ctypes.byref(d)), "cy_server_poll")
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> None:
+        st = lib().cy_server_wait(self.h, ticket, timeout_ms)
+        if st != -7:  # still queued on a timeout: keep its buffers alive
+            self._keep.pop(ticket, None)
+        check(st, "cy_server_wait")
+
+    def drain(self, timeout_ms: int = 600000) -> None:
+        check(lib().cy_server_drain(self.h, timeout_ms), "cy_server_drain")
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        check(lib().cy_server_get_stats(self.h, ctypes.byref(s)), "cy_server_get_stats")
+        return s
+
+    def reset_stats(self) -> None:
+        check(lib().cy_server_reset_stats(self.h), "cy_server_reset_stats")
+
+
+__all__ = ["Server", "Ring", "Yashe", "Workspace", "Graph", "polymul_batched", "polymul_batched_status", "to_limb_array", "from_limb_array", "to_device",
            "to_host", "nlimbs", "CY_OK"]

@@ -1,0 +1,406 @@
+// serve.cpp -- continuous-batching request loop for YASHE homomorphic multiplies.
+//
+// The reference has no serving layer: each Ciphertext::operator* runs alone and
+// synchronises the device (src/ciphertext.cpp:38-73, src/common.h:223). Here a
+// dispatcher thread owns `streams` slots. It
+//   * admits pending requests into a batch of one YASHE context and relin flag
+//     (the oldest request's first, up to max_batch requests, FIFO within them)
+//     when a slot is free and the device-memory budget has room for their
+//     inputs, outputs and residue scratch;
+//   * copies the batch's host ciphertexts into pinned staging, then on the
+//     slot's stream: one host-to-device copy, cy_yashe_mul_ws on the slot's own
+//     workspace, one device-to-host copy, an event;
+//   * retires batches whose event has completed, copies the results to the
+//     callers' buffers, records latencies and frees the budget.
+// Batches of different contexts and sizes run concurrently on different
+// streams while new requests keep arriving. Evaluation keys stay resident in
+// each cy_yashe. Waits are host-side and bounded (cy_server_wait takes a
+// timeout); nothing on the GPU waits on anything.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "host.h"
+
+namespace cy {
+
+static double now_us() {
+    return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    int cls = 0;
+    int relin = 1;
+    const uint64_t* h_c1 = nullptr;
+    const uint64_t* h_c2 = nullptr;
+    uint64_t* h_out = nullptr;
+    double t_submit = 0;
+    bool done = false;
+    cy_status status = CY_OK;
+    size_t bytes = 0;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    cy_workspace ws;
+    bool busy = false;
+    int cls = -1;
+    std::vector<uint64_t> ids;
+    size_t bytes = 0;
+    size_t cap_words = 0;  // uint64 words of one output buffer (inputs hold twice as many)
+    uint64_t *d_in = nullptr, *d_out = nullptr, *h_in = nullptr, *h_out = nullptr;
+    ~Slot() {
+        if (d_in) cudaFree(d_in);
+        if (d_out) cudaFree(d_out);
+        if (h_in) cudaFreeHost(h_in);
+        if (h_out) cudaFreeHost(h_out);
+        if (ev) cudaEventDestroy(ev);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+}  // namespace cy
+
+using namespace cy;
+
+struct cy_server {
+    cy_server_config cfg{};
+    int device = 0;
+    std::vector<cy_yashe*> classes;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<uint64_t> pending;
+    std::unordered_map<uint64_t, Request> reqs;
+    uint64_t next_id = 1;
+    std::vector<std::unique_ptr<Slot>> slots;
+    size_t in_use = 0, peak = 0;
+    bool stop = false;
+    std::thread worker;
+    // statistics
+    std::vector<double> lat_us;
+    uint64_t completed = 0, rejected = 0, batches = 0, failed = 0;
+    double t_first = 0, t_last = 0;
+    ~cy_server();
+};
+
+namespace cy {
+
+static size_t request_bytes(const cy_yashe* y) {
+    const size_t poly = (size_t)y->ring->n * y->ring->l64 * sizeof(uint64_t);
+    const size_t resid = (size_t)std::max(y->tensor.h.k, y->relin.h.k) * y->ring->n * sizeof(uint32_t);
+    return 3 * poly + resid;
+}
+
+// Slots serve every registered context, whose polynomials differ in size:
+// capacity is counted in words, not polynomials.
+static cy_status grow_slot(Slot& s, size_t polys, size_t poly_words) {
+    const size_t words = polys * poly_words;
+    if (words <= s.cap_words) return CY_OK;
+    if (s.d_in) cudaFree(s.d_in);
+    if (s.d_out) cudaFree(s.d_out);
+    if (s.h_in) cudaFreeHost(s.h_in);
+    if (s.h_out) cudaFreeHost(s.h_out);
+    s.d_in = s.d_out = s.h_in = s.h_out = nullptr;
+    s.cap_words = 0;
+    const size_t bytes = words * sizeof(uint64_t);
+    CY_CUDA(cudaMalloc(&s.d_in, 2 * bytes));
+    CY_CUDA(cudaMalloc(&s.d_out, bytes));
+    CY_CUDA(cudaMallocHost(&s.h_in, 2 * bytes));
+    CY_CUDA(cudaMallocHost(&s.h_out, bytes));
+    s.cap_words = words;
+    return CY_OK;
+}
+
+// One pass of the dispatcher. Bookkeeping happens under the lock; copies into
+// and out of the callers' buffers and the launches happen without it, so that
+// submitters are never held up by a batch being prepared. Only this thread
+// touches the slots.
+static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
+    // 1. completed batches: collect under the lock, copy out without it
+    struct Done {
+        Slot* s;
+        cy_status st;
+        std::vector<uint64_t*> outs;
+        size_t poly;
+    };
+    std::vector<Done> done;
+    for (auto& sp : S->slots) {
+        Slot& s = *sp;
+        if (!s.busy) continue;
+        const cudaError_t q = cudaEventQuery(s.ev);
+        if (q == cudaErrorNotReady) continue;
+        Done d{&s, q == cudaSuccess ? CY_OK : cuda_error(q, "serving batch"), {}, 0};
+        const cy_yashe* y = S->classes[s.cls];
+        d.poly = (size_t)y->ring->n * y->ring->l64;
+        if (s.ids.size() * d.poly > s.cap_words) d.st = set_error(CY_ERR_INTERNAL, "serving slot too small");
+        for (uint64_t id : s.ids) d.outs.push_back(S->reqs[id].h_out);
+        done.push_back(std::move(d));
+    }
+    if (!done.empty()) {
+        lock.unlock();
+        for (const Done& d : done)
+            if (d.st == CY_OK)
+                for (size_t i = 0; i < d.outs.size(); i++)
+                    std::memcpy(d.outs[i], d.s->h_out + i * d.poly, d.poly * sizeof(uint64_t));
+        lock.lock();
+        const double t = now_us();
+        for (const Done& d : done) {
+            for (uint64_t id : d.s->ids) {
+                Request& r = S->reqs[id];
+                r.status = d.st;
+                r.done = true;
+                S->lat_us.push_back(t - r.t_submit);
+                if (d.st == CY_OK) S->completed++;
+                else S->failed++;
+            }
+            S->t_last = t;
+            S->in_use -= d.s->bytes;
+            d.s->busy = false;
+            d.s->ids.clear();
+        }
+        S->cv_done.notify_all();
+    }
+
+    // 2. new batches on free slots: choose under the lock, stage and launch without it
+    for (auto& sp : S->slots) {
+        Slot& s = *sp;
+        if (s.busy || S->pending.empty()) continue;
+        const int cls = S->reqs[S->pending.front()].cls;
+        const int relin = S->reqs[S->pending.front()].relin;
+        cy_yashe* y = S->classes[cls];
+        const size_t per = request_bytes(y);
+        std::vector<uint64_t> take;
+        std::vector<const uint64_t*> in1, in2;
+        size_t bytes = 0;
+        for (auto it = S->pending.begin(); it != S->pending.end() && (int)take.size() < S->cfg.max_batch;) {
+            const Request& r = S->reqs[*it];
+            if (r.cls != cls || r.relin != relin) {
+                ++it;
+                continue;
+            }
+            if (S->in_use + bytes + per > S->cfg.device_budget_bytes) break;  // admission by device memory
+            take.push_back(*it);
+            in1.push_back(r.h_c1);
+            in2.push_back(r.h_c2);
+            bytes += per;
+            it = S->pending.erase(it);
+        }
+        if (take.empty()) break;  // the budget is full until a batch retires
+        s.busy = true;  // reserved: not retired before its event is recorded below
+        s.cls = cls;
+        s.ids = take;
+        s.bytes = bytes;
+        S->in_use += bytes;
+        S->peak = std::max(S->peak, S->in_use);
+        S->batches++;
+        lock.unlock();
+        const int nb = (int)take.size();
+        const size_t poly = (size_t)y->ring->n * y->ring->l64;
+        cy_status st = grow_slot(s, nb, poly);
+        if (st == CY_OK && (size_t)nb * poly > s.cap_words) st = set_error(CY_ERR_INTERNAL, "serving slot too small");
+        if (st == CY_OK) {
+            for (int i = 0; i < nb; i++) {
+                std::memcpy(s.h_in + i * poly, in1[i], poly * sizeof(uint64_t));
+                std::memcpy(s.h_in + (nb + i) * poly, in2[i], poly * sizeof(uint64_t));
+            }
+            cudaError_t e = cudaMemcpyAsync(s.d_in, s.h_in, 2 * nb * poly * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                            s.st);
+            if (e != cudaSuccess) st = cuda_error(e, "serving H2D");
+            if (st == CY_OK) st = cy_yashe_mul_ws(y, &s.ws, s.d_in, s.d_in + nb * poly, s.d_out, nb, relin, s.st);
+            if (st == CY_OK) {
+                e = cudaMemcpyAsync(s.h_out, s.d_out, nb * poly * sizeof(uint64_t), cudaMemcpyDeviceToHost, s.st);
+                if (e == cudaSuccess) e = cudaEventRecord(s.ev, s.st);
+                if (e != cudaSuccess) st = cuda_error(e, "serving D2H");
+            }
+        }
+        lock.lock();
+        if (st != CY_OK) {  // fail the batch on the host
+            for (uint64_t id : take) {
+                Request& r = S->reqs[id];
+                r.status = st;
+                r.done = true;
+                S->failed++;
+            }
+            S->in_use -= bytes;
+            s.busy = false;
+            s.ids.clear();
+            S->cv_done.notify_all();
+        }
+    }
+}
+
+static void worker_loop(cy_server* S) {
+    cudaSetDevice(S->device);
+    std::unique_lock<std::mutex> lock(S->mu);
+    while (!S->stop) {
+        dispatch_once(S, lock);
+        bool busy = false;
+        for (auto& s : S->slots) busy |= s->busy;
+        if (busy || !S->pending.empty()) {
+            // poll the slots' events without holding the lock
+            lock.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(S->cfg.poll_us));
+            lock.lock();
+        } else {
+            S->cv_work.wait_for(lock, std::chrono::milliseconds(5));
+        }
+    }
+}
+
+}  // namespace cy
+
+cy_server::~cy_server() {
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        stop = true;
+    }
+    cv_work.notify_all();
+    if (worker.joinable()) worker.join();
+    for (auto& s : slots)
+        if (s->busy) cudaEventSynchronize(s->ev);
+}
+
+extern "C" {
+
+cy_status cy_server_create(const cy_server_config* cfg, cy_server** out) {
+    if (!cfg || !out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cfg->streams < 1 || cfg->streams > 32 || cfg->max_batch < 1 || cfg->device_budget_bytes == 0)
+        return set_error(CY_ERR_INVALID_ARGUMENT, "streams must be 1..32, max_batch >= 1, budget > 0");
+    std::unique_ptr<cy_server> S(new cy_server());
+    S->cfg = *cfg;
+    if (S->cfg.poll_us <= 0) S->cfg.poll_us = 20;
+    CY_CUDA(cudaGetDevice(&S->device));
+    for (int i = 0; i < cfg->streams; i++) {
+        std::unique_ptr<Slot> s(new Slot());
+        CY_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+        CY_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+        s->ws.ws.device = S->device;
+        S->slots.push_back(std::move(s));
+    }
+    S->worker = std::thread(worker_loop, S.get());
+    *out = S.release();
+    return CY_OK;
+}
+
+cy_status cy_server_destroy(cy_server* s) {
+    delete s;
+    return CY_OK;
+}
+
+cy_status cy_server_register(cy_server* S, cy_yashe* y, int* class_id) {
+    if (!S || !y || !class_id) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!y->has_keys) return set_error(CY_ERR_NO_KEYS, "context has no keys");
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->classes.push_back(y);
+    *class_id = (int)S->classes.size() - 1;
+    return CY_OK;
+}
+
+cy_status cy_server_submit(cy_server* S, const cy_serve_request* req, uint64_t* ticket) {
+    if (!S || !req || !ticket) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(S->mu);
+    if (req->class_id < 0 || req->class_id >= (int)S->classes.size() || !req->h_c1 || !req->h_c2 || !req->h_out) {
+        S->rejected++;
+        return set_error(CY_ERR_INVALID_ARGUMENT, "request with an unknown class or NULL buffers");
+    }
+    const size_t bytes = request_bytes(S->classes[req->class_id]);
+    if (bytes > S->cfg.device_budget_bytes) {
+        S->rejected++;
+        return set_error(CY_ERR_OUT_OF_MEMORY, "one request needs more device memory than the whole budget");
+    }
+    Request r;
+    r.cls = req->class_id;
+    r.relin = req->relin ? 1 : 0;
+    r.h_c1 = req->h_c1;
+    r.h_c2 = req->h_c2;
+    r.h_out = req->h_out;
+    r.t_submit = now_us();
+    r.bytes = bytes;
+    if (S->t_first == 0) S->t_first = r.t_submit;
+    const uint64_t id = S->next_id++;
+    S->reqs[id] = r;
+    S->pending.push_back(id);
+    *ticket = id;
+    S->cv_work.notify_one();
+    return CY_OK;
+}
+
+cy_status cy_server_poll(cy_server* S, uint64_t ticket, int* done) {
+    if (!S || !done) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return set_error(CY_ERR_INVALID_ARGUMENT, "unknown ticket");
+    *done = it->second.done ? 1 : 0;
+    return CY_OK;
+}
+
+cy_status cy_server_wait(cy_server* S, uint64_t ticket, int timeout_ms) {
+    if (!S) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::unique_lock<std::mutex> lock(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return set_error(CY_ERR_INVALID_ARGUMENT, "unknown ticket");
+    const bool ok = S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms),
+                                        [&] { return S->reqs[ticket].done; });
+    if (!ok) return set_error(CY_ERR_TIMEOUT, "request not finished before the deadline");
+    const cy_status st = S->reqs[ticket].status;
+    S->reqs.erase(ticket);
+    return st;
+}
+
+cy_status cy_server_drain(cy_server* S, int timeout_ms) {
+    if (!S) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::unique_lock<std::mutex> lock(S->mu);
+    const bool ok = S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), [&] {
+        if (!S->pending.empty()) return false;
+        for (auto& s : S->slots)
+            if (s->busy) return false;
+        return true;
+    });
+    return ok ? CY_OK : set_error(CY_ERR_TIMEOUT, "requests still running at the deadline");
+}
+
+cy_status cy_server_get_stats(cy_server* S, cy_server_stats* out) {
+    if (!S || !out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(S->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->completed = S->completed;
+    out->rejected = S->rejected;
+    out->failed = S->failed;
+    out->batches = S->batches;
+    out->peak_device_bytes = S->peak;
+    std::vector<double> v = S->lat_us;
+    if (!v.empty()) {
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double p) { return v[std::min(v.size() - 1, (size_t)(p * (v.size() - 1) + 0.5))]; };
+        out->p50_us = pct(0.50);
+        out->p99_us = pct(0.99);
+        double sum = 0;
+        for (double x : v) sum += x;
+        out->mean_us = sum / v.size();
+    }
+    if (S->t_last > S->t_first) out->throughput_per_s = S->completed / ((S->t_last - S->t_first) * 1e-6);
+    return CY_OK;
+}
+
+cy_status cy_server_reset_stats(cy_server* S) {
+    if (!S) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->lat_us.clear();
+    S->completed = S->rejected = S->batches = S->failed = 0;
+    S->t_first = S->t_last = 0;
+    S->peak = S->in_use;
+    return CY_OK;
+}
+
+}  // extern "C"

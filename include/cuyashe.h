@@ -242,6 +242,75 @@ cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, 
                        cy_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Serving: continuous batching of HE multiplies                              */
+/* ------------------------------------------------------------------------ */
+
+/* A request loop on the current device. A dispatcher thread admits pending
+ * requests into batches of one registered YASHE context and one relin flag
+ * (oldest request's first, FIFO within them, at most max_batch per batch) whenever one of
+ * `streams` slots is free and device_budget_bytes has room for the batch's
+ * inputs, outputs and scratch; batches of different contexts run concurrently
+ * on different streams while new requests keep arriving. Evaluation keys stay
+ * resident in each cy_yashe. Requests carry host buffers (read when the batch
+ * is formed, written before the request completes; keep them alive until
+ * cy_server_wait returns). Per-request latency (submit to completion) and
+ * throughput are kept for cy_server_get_stats. The reference has no serving layer:
+ * each Ciphertext::operator* runs alone and synchronises the device
+ * (src/ciphertext.cpp:38-73, src/common.h:223). */
+typedef struct cy_server cy_server;
+typedef struct cy_server_config {
+    size_t device_budget_bytes;  /* admission budget for in-flight batches */
+    int streams;                 /* batches in flight at once (1..32) */
+    int max_batch;               /* requests per batch */
+    int poll_us;                 /* dispatcher poll period while batches run (default 20) */
+} cy_server_config;
+typedef struct cy_serve_request {
+    int class_id;                /* from cy_server_register */
+    int relin;                   /* relinearise the product */
+    const uint64_t *h_c1, *h_c2; /* [N][L] ciphertexts of the class's ring */
+    uint64_t *h_out;             /* [N][L] result */
+} cy_serve_request;
+typedef struct cy_server_stats {
+    uint64_t completed, rejected, failed, batches;
+    double p50_us, p99_us, mean_us, throughput_per_s;
+    size_t peak_device_bytes;
+} cy_server_stats;
+
+cy_status cy_server_create(const cy_server_config *cfg, cy_server **out);
+cy_status cy_server_destroy(cy_server *server);
+/* Registers a context that has keys; its requests form their own batches. */
+cy_status cy_server_register(cy_server *server, cy_yashe *y, int *class_id);
+/* Queues a request. Invalid requests (unknown class, NULL buffers) and requests
+ * larger than the whole budget are rejected here and counted. */
+cy_status cy_server_submit(cy_server *server, const cy_serve_request *req, uint64_t *ticket);
+cy_status cy_server_poll(cy_server *server, uint64_t ticket, int *done);
+/* Waits up to timeout_ms; returns the request's status (and forgets the ticket)
+ * or CY_ERR_TIMEOUT (the request stays queued or running). */
+cy_status cy_server_wait(cy_server *server, uint64_t ticket, int timeout_ms);
+/* Waits until nothing is pending or running (CY_ERR_TIMEOUT at the deadline). */
+cy_status cy_server_drain(cy_server *server, int timeout_ms);
+cy_status cy_server_get_stats(cy_server *server, cy_server_stats *stats);
+cy_status cy_server_reset_stats(cy_server *server);
+
+/* ------------------------------------------------------------------------ */
+/* CUDA graphs                                                                */
+/* ------------------------------------------------------------------------ */
+
+/* A fixed batch (fixed buffers) recorded once as a CUDA graph and replayed with
+ * cy_graph_launch: one graph launch instead of one launch per kernel and chunk.
+ * Creation runs the operation once (to size the graph's own workspace), then
+ * captures it on a private stream; it synchronises. Replays of one graph must
+ * not overlap each other on the GPU. The reference synchronises the device
+ * after every operation (src/common.h:223). */
+typedef struct cy_graph cy_graph;
+cy_status cy_polymul_graph_create(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_c, int batch,
+                                  cy_graph **out);
+cy_status cy_yashe_mul_graph_create(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out,
+                                    int batch, int relin, cy_graph **out);
+cy_status cy_graph_launch(cy_graph *graph, cy_stream_t stream);
+cy_status cy_graph_destroy(cy_graph *graph);
+
+/* ------------------------------------------------------------------------ */
 /* Schedule autotuning                                                        */
 /* ------------------------------------------------------------------------ */
 
