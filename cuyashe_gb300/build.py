@@ -38,7 +38,8 @@ def sources():
 
 def headers():
     out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    out.append(os.path.join(ROOT, "include", "cuyashe.h"))
+    inc = os.path.join(ROOT, "include")
+    out += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith((".h", ".hpp"))]
     return out
 
 

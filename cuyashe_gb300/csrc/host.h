@@ -9,7 +9,7 @@
 #include <vector>
 
 #include "../../include/cuyashe.h"
-#include "bigint.h"
+#include "../../include/cuyashe_bigint.h"
 #include "common.h"
 #include "dispatch.h"
 

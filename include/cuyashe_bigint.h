@@ -1,10 +1,11 @@
-// bigint.h -- small arbitrary-precision unsigned integer for host set-up code.
+// cuyashe_bigint.h -- small arbitrary-precision unsigned integer (host only).
 //
 // The reference keeps every wide value in NTL::ZZ on the host (src/polynomial.h,
 // src/integer.h) and in its own bn_t on the device (src/cuda_bn.h:18-23). Here
-// only set-up needs wide host arithmetic: CRT products M, M/p_i, their residues
-// mod q, Barrett constants, keygen. Little-endian 32-bit words, schoolbook
-// multiplication and Knuth's algorithm D for division.
+// host-side wide arithmetic is needed for set-up (CRT products M, M/p_i, their
+// residues mod q, Barrett constants, keygen) and as the coefficient type of the
+// C++ API in cuyashe.hpp. Little-endian 32-bit words, schoolbook multiplication
+// and Knuth's algorithm D for division.
 #pragma once
 
 #include <stdint.h>
@@ -244,6 +245,13 @@ struct BigUInt {
             r = (r * r) % m;
             if (e.bit(i)) r = (r * b) % m;
         }
+        return r;
+    }
+
+    static BigUInt from_dec(const char* s) {
+        BigUInt r;
+        for (; *s; s++)
+            if (*s >= '0' && *s <= '9') r = r * BigUInt(10u) + BigUInt((uint64_t)(*s - '0'));
         return r;
     }
 

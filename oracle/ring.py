@@ -86,7 +86,9 @@ def plain_mul(a: Sequence[int], b: Sequence[int]) -> List[int]:
     n_out = len(a) + len(b) - 1
     ma = max(abs(int(v)) for v in a)
     mb = max(abs(int(v)) for v in b)
-    bound = ma * mb * min(len(a), len(b))  # |c_k| <= bound
+    if ma == 0 or mb == 0:  # the slot width below is sized from a nonzero product
+        return [0] * n_out
+    bound = ma * mb * min(len(a), len(b))  # |c_k| <= bound, and >= every input
     slot_bits = bound.bit_length() + 2
     slot_bytes = (slot_bits + 7) // 8
     slot_bits = 8 * slot_bytes

@@ -109,6 +109,10 @@ def test_kronecker_matches_schoolbook(n):
         ac = [ring.centered(x, q) for x in a]
         bc = [ring.centered(x, q) for x in b]
         assert ring.plain_mul(ac, bc) == ring.plain_mul_schoolbook(ac, bc)
+    # a zero operand against a wide one (YASHE keygen at N = 4 can draw g = 0)
+    wide = [2**126 + 7] * n
+    assert ring.plain_mul([0] * n, wide) == [0] * (2 * n - 1)
+    assert ring.plain_mul(wide, [0] * n) == [0] * (2 * n - 1)
 
 
 @pytest.mark.parametrize("n", [4, 64, 1024])
