@@ -36,6 +36,7 @@ T = 1024
 W_BITS = 32
 L = 2                                               # uint64 limbs per coefficient
 CT_BYTES = N * L * 8                                # one ciphertext / polynomial
+DEEP_N, DEEP_T, DEEP_PAIRS = 16384, 65537, 64       # the deep-level workload
 
 
 def log(*a):
@@ -284,14 +285,14 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
 # our arm
 # ----------------------------------------------------------------------------
 
-def make_inputs(Y, batch: int, pool: int, seed: int):
+def make_inputs(Y, batch: int, pool: int, seed: int, n: int = N, t: int = T):
     """Fresh encryptions (library keygen + encryption), tiled to `batch` pairs."""
     import numpy as np
     import torch
 
     rng = np.random.default_rng(seed)
-    m1 = rng.integers(0, T, size=(pool, N), dtype=np.uint64)
-    m2 = rng.integers(0, T, size=(pool, N), dtype=np.uint64)
+    m1 = rng.integers(0, t, size=(pool, n), dtype=np.uint64)
+    m2 = rng.integers(0, t, size=(pool, n), dtype=np.uint64)
     ct1 = Y.encrypt_host(m1, seed=seed + 1)
     ct2 = Y.encrypt_host(m2, seed=seed + 2)
     idx1 = np.arange(batch) % pool
@@ -299,6 +300,48 @@ def make_inputs(Y, batch: int, pool: int, seed: int):
     C1 = torch.from_numpy(ct1.view(np.int64)).cuda()[torch.from_numpy(idx1).cuda()].contiguous()
     C2 = torch.from_numpy(ct2.view(np.int64)).cuda()[torch.from_numpy(idx2).cuda()].contiguous()
     return C1, C2, m1, m2, idx1, idx2
+
+
+def deep_bench(cy, steps: int, stream):
+    """The deep-level workload: 64 HE multiplies with relinearisation at
+    N = 16384, a 380-bit q (the largest prime below 2^380 that is 1 mod 2^16),
+    t = 65537, w = 2^32 (12 digits). Its inputs (100 MB) fit in L2, so every
+    step is timed alone with CUDA events after a write of a buffer larger than
+    L2, and the step times are summed."""
+    import numpy as np
+    import torch
+
+    q = _q380()
+    Y = cy.Yashe(DEEP_N, q, DEEP_T, W_BITS, 8.0)
+    Y.keygen(4242)
+    C1, C2, m1, m2, i1, i2 = make_inputs(Y, DEEP_PAIRS, pool=4, seed=31, n=DEEP_N, t=DEEP_T)
+    OUT = Y.ring.empty(DEEP_PAIRS)
+
+    def step():
+        Y.mul(C1, C2, relin=True, out=OUT)
+
+    step()
+    dec = Y.decrypt(OUT[:2]).cpu().numpy().view(np.uint64)
+    PT = cy.Ring(DEEP_N, DEEP_T)
+    exp = PT.polymul(PT.upload(m1[i1[:2]].astype(object).tolist()),
+                     PT.upload(m2[i2[:2]].astype(object).tolist()))
+    exp = exp.cpu().numpy().view(np.uint64)[..., 0]
+    ok = bool((dec == exp).all())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        step()
+    total = 0.0
+    for _ in range(steps):
+        flush.fill_(1)
+        total += time_steps(step, 1, stream)
+    with cy.Trace() as tr:
+        step()
+    kernels = {name: {"launches": cnt, "ms": round(kms, 4)} for name, (cnt, kms) in tr.kernels.items()}
+    info = Y.info()
+    return {"workload": "yashe_mul_relin N=16384 log2q=%d t=%d w=2^32 ell=%d" % (q.bit_length(), DEEP_T, info.ell),
+            "pairs": DEEP_PAIRS, "he_mults_per_s": DEEP_PAIRS * steps / (total / 1000.0),
+            "ms_per_step": total / steps, "tensor_primes": info.tensor_primes, "relin_primes": info.relin_primes,
+            "l2": "256 MB written between timed steps", "kernels": kernels, "decrypt_check": ok}
 
 
 def time_steps(fn, steps: int, stream):
@@ -335,14 +378,10 @@ def run_ours(args):
 
     import cuyashe_gb300 as cy
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cuyashe_gb300 import replicas
+
+    rep = replicas.from_env("nccl")  # replicas: no data-path collective
+    world, rank, local = rep.world, rep.rank, rep.local
     cy.lib()
     stream = torch.cuda.current_stream()
     B = args.batch
@@ -382,22 +421,16 @@ def run_ours(args):
 
     # ---- timed region -----------------------------------------------------------
     launches0 = cy.launch_count()
-    if dist:
-        dist.barrier()
+    replicas.barrier(rep)
     with ClockSampler(local) as clocks:
         ms = time_steps(step, args.steps, stream)
     launches = cy.launch_count() - launches0
-    ms_t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = replicas.max_over_ranks(rep, ms)
     value = world * B * args.steps / (ms_max / 1000.0)
     log("batched HE mults/s: %.1f (%.3f ms/step, batch %d)" % (value, ms_max / args.steps, B))
 
     if rank != 0:
-        if dist:
-            dist.barrier()
-            dist.destroy_process_group()
+        replicas.close(rep)
         return
 
     # ---- per-kernel device times (one traced step, outside the timed region) ----
@@ -536,6 +569,15 @@ def run_ours(args):
     except Exception as e:  # reported, not fatal for the headline
         log("mixed batch failed:", e)
 
+    # ---- deep level: N = 16384, 380-bit q, 64 pairs ------------------------------
+    deep = None
+    if not args.no_deep:
+        try:
+            deep = deep_bench(cy, max(3, args.steps // 2), stream)
+            log("deep:", deep)
+        except Exception as e:
+            log("deep bench failed:", e)
+
     # ---- serving: Poisson arrivals of mixed-size multiplies --------------------
     serving = None
     if not args.no_serving:
@@ -598,15 +640,14 @@ def run_ours(args):
         "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
                     "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
         "mixed_batch": mixed,
+        "deep_level": deep,
         "cuda_graph": graphs,
         "serving": serving,
         "decrypt_check": decrypt_ok,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    replicas.close(rep)
 
 
 def main():
@@ -618,6 +659,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT schedules")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-deep", action="store_true", help="skip the N=16384 / 380-bit measurement")
     ap.add_argument("--serving-only", type=float, default=0.0, metavar="SECONDS",
                     help="run only the serving measurement over SECONDS of arrivals and print it")
     ap.add_argument("--ncu-step", action="store_true",
