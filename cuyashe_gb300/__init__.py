@@ -122,6 +122,7 @@ SIGNATURES = {
     "cy_yashe_decrypt": ([_vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_mul": ([_vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_mul_ws": ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
+    "cy_yashe_mul_host": ([_vp, _vp, _vp, _vp, _i, _i], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
     "cy_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)], _i),

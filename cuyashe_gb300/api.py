@@ -44,6 +44,18 @@ def from_limb_array(arr: np.ndarray):
     return np.array(vals, dtype=object).reshape(a.shape[:-1])
 
 
+def _host_ptr(x) -> int:
+    """Address of a C-contiguous host array of 8-byte words: a numpy array, or a
+    CPU torch tensor (page-locked ones let the copies overlap the kernels)."""
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous or x.dtype.itemsize != 8:
+            raise ValueError("host arrays must be C-contiguous with 8-byte elements")
+        return x.ctypes.data
+    if x.device.type != "cpu" or not x.is_contiguous() or x.element_size() != 8:
+        raise ValueError("host tensors must be contiguous CPU tensors with 8-byte elements")
+    return x.data_ptr()
+
+
 def to_device(arr: np.ndarray, device="cuda"):
     import torch
     a = np.ascontiguousarray(arr, dtype=np.uint64)
@@ -133,11 +145,14 @@ class Ring:
             check(lib().cy_polymul_ws(self.h, workspace.h, _ptr(a), _ptr(b), _ptr(out), batch, st), "cy_polymul_ws")
         return out
 
-    def polymul_host(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
-        a = np.ascontiguousarray(a, dtype=np.uint64)
-        b = np.ascontiguousarray(b, dtype=np.uint64)
-        out = np.empty_like(a)
-        check(lib().cy_polymul_host(self.h, a.ctypes.data, b.ctypes.data, out.ctypes.data, a.shape[0]),
+    def polymul_host(self, a, b, out=None):
+        """a*b with a, b, out in host memory ([batch][N][L] words: numpy arrays or
+        CPU torch tensors)."""
+        if isinstance(a, np.ndarray):
+            a = np.ascontiguousarray(a, dtype=np.uint64)
+            b = np.ascontiguousarray(b, dtype=np.uint64)
+        out = (np.empty_like(a) if isinstance(a, np.ndarray) else a.new_empty(a.shape)) if out is None else out
+        check(lib().cy_polymul_host(self.h, _host_ptr(a), _host_ptr(b), _host_ptr(out), a.shape[0]),
               "cy_polymul_host")
         return out
 
@@ -277,6 +292,17 @@ class Yashe:
         else:
             check(lib().cy_yashe_mul_ws(self.h, workspace.h, _ptr(c1), _ptr(c2), _ptr(out), c1.shape[0],
                                         1 if relin else 0, st), "cy_yashe_mul_ws")
+        return out
+
+    def mul_host(self, c1, c2, out=None, relin: bool = True):
+        """The HE multiply on host buffers (numpy arrays or CPU torch tensors,
+        [batch][N][L] words); returns once `out` is written."""
+        if isinstance(c1, np.ndarray):
+            c1 = np.ascontiguousarray(c1, dtype=np.uint64)
+            c2 = np.ascontiguousarray(c2, dtype=np.uint64)
+        out = (np.empty_like(c1) if isinstance(c1, np.ndarray) else c1.new_empty(c1.shape)) if out is None else out
+        check(lib().cy_yashe_mul_host(self.h, _host_ptr(c1), _host_ptr(c2), _host_ptr(out), c1.shape[0],
+                                      1 if relin else 0), "cy_yashe_mul_host")
         return out
 
     def mul_graph(self, c1, c2, out, relin: bool = True) -> Graph:

@@ -42,7 +42,7 @@ static long long chunk_bytes() {
     }();
     return v;
 }
-static int chunk_jobs(int n, int k) {
+int chunk_jobs(int n, int k) {
     long long c = chunk_bytes() / ((long long)n * k * 4);
     if (c < 1) c = 1;
     if (c > 65535) c = 65535;
@@ -362,22 +362,9 @@ cy_status cy_polymul(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint6
 cy_status cy_polymul_host(cy_ring* r, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_c, int batch) {
     CY_TRY(validate_poly_args(r, h_a, h_b, h_c, batch));
     if (batch == 0) return CY_OK;
-    const size_t bytes = sizeof(uint64_t) * (size_t)batch * r->n * r->l64;
-    uint64_t *a = nullptr, *b = nullptr, *c = nullptr;
-    cudaError_t e = cudaMalloc(&a, bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&b, bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&c, bytes);
-    cy_status st = CY_OK;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(a, h_a, bytes, cudaMemcpyHostToDevice, 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b, h_b, bytes, cudaMemcpyHostToDevice, 0);
-    if (e == cudaSuccess) st = cy_polymul(r, a, b, c, batch, 0);
-    if (e == cudaSuccess && st == CY_OK) e = cudaMemcpyAsync(h_c, c, bytes, cudaMemcpyDeviceToHost, 0);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
-    cudaFree(a);
-    cudaFree(b);
-    cudaFree(c);
-    if (e != cudaSuccess) return cuda_error(e, "cy_polymul_host");
-    return st;
+    return run_host_pipeline((size_t)r->n * r->l64, batch, chunk_jobs(r->n, r->mul.h.k), h_a, h_b, h_c,
+                             [r](cy_workspace* ws, const uint64_t* a, const uint64_t* b, uint64_t* c, int nj,
+                                 cudaStream_t st) { return cy_polymul_ws(r, ws, a, b, c, nj, st); });
 }
 
 cy_status cy_polyadd(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_c, int batch,

@@ -193,6 +193,18 @@ cy_status cy_yashe_mul(cy_yashe* y, const uint64_t* d_c1, const uint64_t* d_c2, 
     return cy_yashe_mul_ws(y, nullptr, d_c1, d_c2, d_out, batch, relin, stream);
 }
 
+cy_status cy_yashe_mul_host(cy_yashe* y, const uint64_t* h_c1, const uint64_t* h_c2, uint64_t* h_out, int batch,
+                            int relin) {
+    CY_TRY(yashe_check(y, h_c1, h_c2, batch));
+    if (batch > 0 && !h_out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL buffer");
+    if (relin && !y->has_keys) return set_error(CY_ERR_NO_KEYS, "relinearisation needs keys");
+    if (batch == 0) return CY_OK;
+    cy_ring* r = y->ring;
+    return run_host_pipeline((size_t)r->n * r->l64, batch, chunk_jobs(r->n, y->tensor.h.k), h_c1, h_c2, h_out,
+                             [y, relin](cy_workspace* ws, const uint64_t* a, const uint64_t* b, uint64_t* c, int nj,
+                                        cudaStream_t st) { return cy_yashe_mul_ws(y, ws, a, b, c, nj, relin, st); });
+}
+
 cy_status cy_yashe_keyswitch(cy_yashe* y, const uint64_t* d_c, uint64_t* d_out, int batch, cy_stream_t stream) {
     CY_TRY(yashe_check(y, d_c, d_out, batch));
     if (!y->has_keys) return set_error(CY_ERR_NO_KEYS, "no keys installed");

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -73,6 +74,17 @@ struct Workspace {
     cy_status reserve(size_t words);
     ~Workspace();
 };
+
+// Jobs per launch of the product kernels (residue scratch near CY_CHUNK_BYTES).
+int chunk_jobs(int n, int k);
+
+// Host-buffer calls (hostpipe.cpp): `batch` jobs of `words` uint64 words per
+// operand, `chunk` jobs at a time through three device slots, copies
+// overlapping the kernels. op(ws, d_in0, d_in1, d_out, jobs, stream) runs one
+// chunk; h_in1 may be NULL for a one-operand call.
+using ChunkOp = std::function<cy_status(cy_workspace*, const uint64_t*, const uint64_t*, uint64_t*, int, cudaStream_t)>;
+cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* h_in0, const uint64_t* h_in1,
+                            uint64_t* h_out, const ChunkOp& op);
 
 }  // namespace cy
 

@@ -102,8 +102,11 @@ cy_status cy_polymul(cy_ring *ring, const uint64_t *d_a, const uint64_t *d_b, ui
 cy_status cy_polymul_ws(cy_ring *ring, cy_workspace *ws, const uint64_t *d_a, const uint64_t *d_b,
                         uint64_t *d_c, int batch, cy_stream_t stream);
 
-/* Same product with host buffers: copies in, multiplies, copies out, and
- * synchronises (the reference's with-memcopy path, src/benchmark_polynomial.cpp:361-388). */
+/* Same product with host buffers; returns once h_c is written (the
+ * reference's with-memcopy path, src/benchmark_polynomial.cpp:361-388). The
+ * batch runs in chunks whose copies overlap the kernels of neighbouring chunks
+ * when the buffers are page-locked; pageable buffers give the same result
+ * without the overlap. */
 cy_status cy_polymul_host(cy_ring *ring, const uint64_t *h_a, const uint64_t *h_b, uint64_t *h_c, int batch);
 
 /* c = a + b mod q and c = a - b mod q, elementwise over the batch.
@@ -233,6 +236,17 @@ cy_status cy_yashe_mul(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, 
                        int relin, cy_stream_t stream);
 cy_status cy_yashe_mul_ws(cy_yashe *y, cy_workspace *ws, const uint64_t *d_c1, const uint64_t *d_c2,
                           uint64_t *d_out, int batch, int relin, cy_stream_t stream);
+
+/* cy_yashe_mul on HOST buffers c1, c2, out ([batch][N][L] limbs); returns once
+ * out is written. The batch runs in chunks whose host<->device copies overlap
+ * the kernels of neighbouring chunks when the buffers are page-locked
+ * (cudaHostAlloc / cudaHostRegister); pageable buffers give the same result
+ * without the overlap. Replaces Ciphertext::operator* on host-resident
+ * operands, i.e. update_device_data, the product and update_host_data
+ * (src/ciphertext.cpp:38-73, src/polynomial.cpp:265-417). Calls on one device
+ * share one pipeline and run one after another. */
+cy_status cy_yashe_mul_host(cy_yashe *y, const uint64_t *h_c1, const uint64_t *h_c2, uint64_t *h_out, int batch,
+                            int relin);
 
 /* Relinearisation alone: out = [sum_d D_d(c)*evk_d]_q (Ciphertext::convert). */
 cy_status cy_yashe_keyswitch(cy_yashe *y, const uint64_t *d_c, uint64_t *d_out, int batch, cy_stream_t stream);
