@@ -319,6 +319,7 @@ def deep_bench(cy, steps: int, stream):
     q = _q380()
     Y = cy.Yashe(DEEP_N, q, DEEP_T, W_BITS, 8.0)
     Y.keygen(4242)
+    Y.autotune(batch=DEEP_PAIRS)
     C1, C2, m1, m2, i1, i2 = make_inputs(Y, DEEP_PAIRS, pool=4, seed=31, n=DEEP_N, t=DEEP_T)
     OUT = Y.ring.empty(DEEP_PAIRS)
 
@@ -610,6 +611,13 @@ def run_ours(args):
     e2e_ms = (time.perf_counter() - t0) * 1000.0
     e2e_rate = B * e2e_steps / (e2e_ms / 1000.0)
     e2e_ok = torch.equal(HO, OUT.cpu())
+    # copy bandwidth on its own (what bounds e2e when the copies outlast the kernels)
+    Dtmp = torch.empty_like(C1)
+    h2d_ms = time_steps(lambda: Dtmp.copy_(H1, non_blocking=True), 5, stream)
+    d2h_ms = time_steps(lambda: HO.copy_(OUT, non_blocking=True), 5, stream)
+    copy_gbs = {"h2d_gbs": 5 * B * CT_BYTES / (h2d_ms / 1000.0) / 1e9,
+                "d2h_gbs": 5 * B * CT_BYTES / (d2h_ms / 1000.0) / 1e9}
+    del Dtmp
 
     # ---- CPU baseline: the reference's multiply on the host cores ---------------
     cpu = None
@@ -637,7 +645,7 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_rate, "unit": "HE mults/s", "h2d_bytes_per_step": 2 * B * CT_BYTES,
                 "d2h_bytes_per_step": B * CT_BYTES, "output_matches_device": e2e_ok,
-                "api": "cy_yashe_mul_host (page-locked host buffers, host wall clock)"},
+                "api": "cy_yashe_mul_host (page-locked host buffers, host wall clock)", "copy_alone": copy_gbs},
         "gpu_launches": launches,
         "roofline": roofline,
         "step_roofline": {"bound": "hbm", "achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",

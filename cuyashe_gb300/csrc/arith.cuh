@@ -7,17 +7,16 @@
 //   * Shoup multiplication by a precomputed constant (twiddles, CRT factors):
 //     one mul.hi and two mul.lo, result in [0, 2p) for any 32-bit input;
 //   * Montgomery multiplication for the pointwise product of two variables;
-//   * lazy reduction with the unsigned-min trick min(x, x - m).
+//   * lazy reduction with the unsigned-min trick min(x, x - m), written with the
+//     add-then-min intrinsic __viaddmin_u32 so that it is one instruction.
 #pragma once
 
 #include <stdint.h>
 
 namespace cy {
 
-__device__ __forceinline__ uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
-
 // x in [0, 2m) -> [0, m)   (x - m wraps above x when x < m)
-__device__ __forceinline__ uint32_t red(uint32_t x, uint32_t m) { return umin32(x, x - m); }
+__device__ __forceinline__ uint32_t red(uint32_t x, uint32_t m) { return __viaddmin_u32(x, 0u - m, x); }
 
 // x * w mod p in [0, 2p), any 32-bit x; w < p, ws = floor(w * 2^32 / p), p < 2^31.
 __device__ __forceinline__ uint32_t shoup(uint32_t x, uint32_t w, uint32_t ws, uint32_t p) {
@@ -45,7 +44,7 @@ __device__ __forceinline__ void ct_bfly(uint32_t& X, uint32_t& Y, uint32_t w, ui
 // Gentleman-Sande butterfly: X, Y in [0, 2p) -> X + Y, (X - Y) w in [0, 2p).
 __device__ __forceinline__ void gs_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, uint32_t p) {
     const uint32_t p2 = 2 * p;
-    const uint32_t s = red(X + Y, p2);
+    const uint32_t s = red(X + Y, p2);  // one add, one add-then-min
     const uint32_t d = X - Y + p2;
     Y = shoup(d, w, ws, p);
     X = s;

@@ -16,6 +16,10 @@ void fill_n12_e4(KernelSet& ks);
 void fill_n13_e3(KernelSet& ks);
 void fill_n13_e4(KernelSet& ks);
 void fill_n14_e4(KernelSet& ks);
+void fill_n12_e3r(KernelSet& ks);
+void fill_n12_e4r(KernelSet& ks);
+void fill_n13_e4r(KernelSet& ks);
+void fill_n14_e5(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -43,6 +47,11 @@ static const VariantTable& variants() {
         add(13, fill_n13_e4);
         add(13, fill_n13_e3);
         add(14, fill_n14_e4);
+        // larger register budgets per thread (fewer blocks per SM)
+        add(12, fill_n12_e3r);
+        add(12, fill_n12_e4r);
+        add(13, fill_n13_e4r);
+        add(14, fill_n14_e5);
     });
     return T;
 }

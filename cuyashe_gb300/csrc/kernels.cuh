@@ -125,9 +125,15 @@ __device__ __forceinline__ uint32_t crt_words(const uint32_t (&w)[W], const uint
         acc = (j0 == 0) ? f : red(acc + f, 2 * c.p);
     }
     if (CENTER) {
-        bool gt = false;
+        // x > (q-1)/2: the top words decide unless they are equal (rare), then
+        // the lower words do
+        bool gt = w[W - 1] > qh[W - 1];
+        if (w[W - 1] == qh[W - 1]) {
+            bool g = false;
 #pragma unroll
-        for (int j = 0; j < W; j++) gt = (w[j] > qh[j]) || (w[j] == qh[j] && gt);
+            for (int j = 0; j < W - 1; j++) g = (w[j] > qh[j]) || (w[j] == qh[j] && g);
+            gt = g;
+        }
         if (gt) acc = acc + 2 * c.p - c.qmodp;  // [0, 4p)
     }
     return acc;
@@ -153,8 +159,10 @@ constexpr int ks_min_blocks() {
     return target < 1 ? 1 : (target > 16 ? 16 : target);
 }
 
-template <int LOGN, int LOGE, int L64, bool CENTER>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (mul_min_blocks<LOGN, LOGE>()))
+// MINB > 0 overrides the blocks per SM the kernel is compiled for (a schedule
+// with a larger register budget per thread).
+template <int LOGN, int LOGE, int L64, bool CENTER, int MINB = 0>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul_min_blocks<LOGN, LOGE>()))
     k_mul(const BasisDev* __restrict__ B, const uint64_t* __restrict__ A, long long a_stride,
           const uint64_t* __restrict__ Bv, long long b_stride, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -219,8 +227,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (mul_min_blocks<LOGN, 
 // coefficients of c in [0, q) (w = 2^32), processed ND at a time.
 // evk: [ell][k][N] (value, Shoup companion) in the forward-NTT output order.
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, int L64, int ND>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (ks_min_blocks<LOGN, LOGE>()))
+template <int LOGN, int LOGE, int L64, int ND, int MINB = 0>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_min_blocks<LOGN, LOGE>()))
     k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
                 int ell, uint32_t* __restrict__ resid) {
     using PL = NttPlan<LOGN, LOGE>;
@@ -432,28 +440,35 @@ __device__ __forceinline__ uint64_t barrett(const Cols<L>& x, const uint32_t* qn
     return Q;
 }
 
+// Epilogue constants in shared memory. The per-prime rows are padded to a
+// multiple of three primes with zero factors (ycon = 0, zero rows), so that a
+// padded prime contributes exactly nothing and the prime loop runs whole
+// groups of three without guards.
+constexpr int KPAD = KMAX + 2;
 struct EpiShared {
-    uint32_t p[KMAX], ycon[KMAX], ycon_sh[KMAX], flo[KMAX], fhi[KMAX];
-    uint32_t A0[KMAX * L32MAX];
-    uint32_t A1[KMAX * L32MAX];
+    uint32_t p[KPAD], ycon[KPAD], ycon_sh[KPAD], flo[KPAD], fhi[KPAD];
+    uint32_t A0[KPAD * L32MAX];
+    uint32_t A1[KPAD * L32MAX];
     uint32_t B0[L32MAX], B1[L32MAX], qn[L32MAX], qhalf_n[L32MAX];
 };
 
 // Copy the epilogue constants of basis B into shared memory (threads tid, tid +
-// nthreads, ... of the caller's group).
+// nthreads, ... of the caller's group), with the zero padding up to 3*ceil(k/3).
 template <int L, int MODE>
 __device__ __forceinline__ void epi_stage(EpiShared& S, const BasisDev* __restrict__ B, int tid, int nthreads) {
-    const int k = B->k;
-    for (int i = tid; i < k; i += nthreads) {
-        S.p[i] = B->p[i];
-        S.ycon[i] = B->ycon[i];
-        S.ycon_sh[i] = B->ycon_sh[i];
-        S.flo[i] = B->flo[i];
-        S.fhi[i] = B->fhi[i];
+    const int k = B->k, kp = 3 * ((k + 2) / 3);
+    for (int i = tid; i < kp; i += nthreads) {
+        const bool in = i < k;
+        S.p[i] = in ? B->p[i] : 1u;
+        S.ycon[i] = in ? B->ycon[i] : 0u;
+        S.ycon_sh[i] = in ? B->ycon_sh[i] : 0u;
+        S.flo[i] = in ? B->flo[i] : 0u;
+        S.fhi[i] = in ? B->fhi[i] : 0u;
     }
-    for (int i = tid; i < k * L; i += nthreads) {
-        S.A0[i] = B->A0[i / L][i % L];
-        if (MODE == EPI_YASHE) S.A1[i] = B->A1[i / L][i % L];
+    for (int i = tid; i < kp * L; i += nthreads) {
+        const bool in = i < k * L;
+        S.A0[i] = in ? B->A0[i / L][i % L] : 0u;
+        if (MODE == EPI_YASHE) S.A1[i] = in ? B->A1[i / L][i % L] : 0u;
     }
     for (int i = tid; i < L; i += nthreads) {
         S.B0[i] = B->B0[i];
@@ -470,6 +485,7 @@ template <int L, int MODE>
 __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __restrict__ B,
                                          const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst) {
     const int k = B->k, shift = B->shift, l64 = B->l64;
+    const int groups = (k + 2) / 3;
     const uint64_t mu = B->mu;
     Cols<L> c0, c1;
     c0.zero();
@@ -484,29 +500,27 @@ __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __r
         c0.mac(y, &S.A0[i * L]);
         if (MODE == EPI_YASHE) c1.mac(y, &S.A1[i * L]);
     };
-    // Issue the loads of the first KU residues together (they come from L2), then
-    // absorb them; columns take three products of < 2^62 between carry passes.
-    constexpr int KU = 15;
-    uint32_t rk[KU];
+    // Residues come from L2: the loads of the next two groups of three primes are
+    // in flight while a group is absorbed. Loads past the last prime re-read its
+    // residue (a valid address); its padded factors make the contribution zero.
+    auto load3 = [&](int g, uint32_t (&d)[3]) {
 #pragma unroll
-    for (int i = 0; i < KU; i++) rk[i] = (i < k) ? __ldcg(r0 + (size_t)i * stride) : 0u;
+        for (int j = 0; j < 3; j++) d[j] = __ldcg(r0 + (size_t)min(3 * g + j, k - 1) * stride);
+    };
+    uint32_t g0[3], g1[3], g2[3];
+    load3(0, g0);
+    load3(min(1, groups - 1), g1);
+    for (int g = 0; g < groups; g++) {
+        load3(min(g + 2, groups - 1), g2);
 #pragma unroll
-    for (int i = 0; i < KU; i++) {
-        if (i < k) absorb(i, rk[i]);
-        if (i % 3 == 2) {
-            c0.norm();
-            if (MODE == EPI_YASHE) c1.norm();
-        }
-    }
-    for (int i0 = KU; i0 < k; i0 += 3) {  // bases of more than KU primes
-        uint32_t rr[3];
-#pragma unroll
-        for (int j = 0; j < 3; j++) rr[j] = (i0 + j < k) ? __ldcg(r0 + (size_t)(i0 + j) * stride) : 0u;
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            if (i0 + j < k) absorb(i0 + j, rr[j]);
-        c0.norm();
+        for (int j = 0; j < 3; j++) absorb(3 * g + j, g0[j]);
+        c0.norm();  // columns take three products of < 2^62 between carry passes
         if (MODE == EPI_YASHE) c1.norm();
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            g0[j] = g1[j];
+            g1[j] = g2[j];
+        }
     }
     const uint32_t v = (uint32_t)((vacc + 0x80000000ULL) >> 32);  // round(sum y_i/p_i): X = sum y_i Mhat_i - v M
     c0.norm();
@@ -575,28 +589,30 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
 
 namespace cy {
 
-template <int LOGN, int LOGE, int L64>
+template <int LOGN, int LOGE, int L64, int MB_MUL, int MB_KS>
 void fill_l64(KernelSet& ks) {
-    ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false>;
-    ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true>;
-    ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, 2>;
-    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4>;
+    ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false, MB_MUL>;
+    ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true, MB_MUL>;
+    ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, 2, MB_KS>;
+    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4, MB_KS>;
 }
 
 // SPECIALISE: also instantiate the kernels for 1, 2, 3 and 6 limbs (q of up to
 // 64, 128, 192 and 384 bits); other limb counts use the generic kernels.
-template <int LOGN, int LOGE, bool SPECIALISE>
+// MB_MUL / MB_KS > 0: blocks per SM the product / keyswitch kernels are
+// compiled for (0: the defaults above).
+template <int LOGN, int LOGE, bool SPECIALISE, int MB_MUL = 0, int MB_KS = 0>
 void fill_kernel_set(KernelSet& ks) {
     using PL = NttPlan<LOGN, LOGE>;
     ks.logn = LOGN;
     ks.loge = LOGE;
     ks.threads = PL::G;
-    fill_l64<LOGN, LOGE, 0>(ks);
+    fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS>(ks);
     if constexpr (SPECIALISE) {
-        fill_l64<LOGN, LOGE, 1>(ks);
-        fill_l64<LOGN, LOGE, 2>(ks);
-        fill_l64<LOGN, LOGE, 3>(ks);
-        fill_l64<LOGN, LOGE, 6>(ks);
+        fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS>(ks);
+        fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS>(ks);
+        fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS>(ks);
+        fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS>(ks);
     }
     ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
     ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
