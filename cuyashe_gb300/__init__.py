@@ -123,6 +123,8 @@ SIGNATURES = {
     "cy_yashe_mul": ([_vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_mul_ws": ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     "cy_yashe_mul_host": ([_vp, _vp, _vp, _vp, _i, _i], _i),
+    "cy_yashe_encrypt": ([_vp, _vp, _vp, _i, ctypes.c_uint64, _vp], _i),
+    "cy_gaussian_cdt": ([ctypes.c_double, _u64p, _i, ctypes.POINTER(_i)], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
     "cy_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)], _i),

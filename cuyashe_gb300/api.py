@@ -276,6 +276,14 @@ class Yashe:
               "cy_yashe_encrypt_host")
         return ct
 
+    def encrypt(self, m, seed: int, out=None, stream=None):
+        """GPU encryption of device plaintexts m ([batch][N] uint64 words, a CUDA
+        tensor) with s and e sampled on the GPU (counter-based, seeded)."""
+        out = self.ring.empty(m.shape[0]) if out is None else out
+        check(lib().cy_yashe_encrypt(self.h, _ptr(m), _ptr(out), m.shape[0], seed, _stream_handle(stream)),
+              "cy_yashe_encrypt")
+        return out
+
     def decrypt(self, ct, aftermul: bool = False, stream=None):
         import torch
         out = torch.empty((ct.shape[0], self.n), dtype=torch.int64, device=ct.device)

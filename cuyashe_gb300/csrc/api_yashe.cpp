@@ -34,6 +34,8 @@ using namespace cy;
 cy_yashe::~cy_yashe() {
     if (d_f) cudaFree(d_f);
     if (d_f2) cudaFree(d_f2);
+    if (d_h) cudaFree(d_h);
+    if (d_cdt) cudaFree(d_cdt);
     if (d_evk) cudaFree(d_evk);
     if (ring) cy_ring_destroy(ring);
 }
@@ -126,7 +128,9 @@ cy_status cy_yashe_set_keys(cy_yashe* y, const uint64_t* h_f, const uint64_t* h_
     y->has_keys = false;
     if (!y->d_f) CY_CUDA(cudaMalloc(&y->d_f, poly * sizeof(uint64_t)));
     if (!y->d_f2) CY_CUDA(cudaMalloc(&y->d_f2, poly * sizeof(uint64_t)));
+    if (!y->d_h) CY_CUDA(cudaMalloc(&y->d_h, poly * sizeof(uint64_t)));
     CY_CUDA(cudaMemcpy(y->d_f, h_f, poly * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    CY_CUDA(cudaMemcpy(y->d_h, h_h, poly * sizeof(uint64_t), cudaMemcpyHostToDevice));
     CY_TRY(cy_polymul(r, y->d_f, y->d_f, y->d_f2, 1, nullptr));
     if (y->d_evk) {
         cudaFree(y->d_evk);

@@ -117,6 +117,9 @@ struct cy_yashe {
     std::vector<uint64_t> h_f, h_h, h_evk;
     uint64_t* d_f = nullptr;
     uint64_t* d_f2 = nullptr;
-    uint2* d_evk = nullptr;  // [ell][k'][N] NTT-domain evaluation key
+    uint64_t* d_h = nullptr;    // public key (GPU encryption)
+    uint2* d_evk = nullptr;     // [ell][k'][N] NTT-domain evaluation key
+    uint64_t* d_cdt = nullptr;  // discrete Gaussian thresholds (GPU sampling)
+    int n_cdt = 0;
     ~cy_yashe();
 };

@@ -221,6 +221,24 @@ cy_status cy_yashe_get_keys(const cy_yashe *y, uint64_t *h_f, uint64_t *h_h, uin
  * [0, t); ct: [batch][N][L]. Replaces Yashe::encrypt (src/yashe.cpp:104-142). */
 cy_status cy_yashe_encrypt_host(cy_yashe *y, const uint64_t *h_m, uint64_t *h_ct, int batch, uint64_t seed);
 
+/* Encryption on the GPU: ct = [h*s + e + Delta*(m mod t)]_q, Delta = floor(q/t),
+ * with s and e drawn on the GPU from the discrete Gaussian of width sigma on
+ * [-B, B], B = ceil(6 sigma). Draw c of a call is the c-th output of
+ * splitmix64 seeded with `seed` (mix(seed + (c+1) * 0x9E3779B97F4A7C15));
+ * coefficient i of s (of e) of ciphertext b uses c = 2b*N + i ((2b+1)*N + i),
+ * mapped through the 64-bit CDT thresholds T_j = floor(2^64 * sum_{x<=j-B}
+ * w_x / sum w), w_x = exp(-x^2 / (2 sigma^2)), to the first j with draw < T_j.
+ * d_m: [batch][N] uint64; d_ct: [batch][N][L]. Asynchronous on `stream`.
+ * Replaces Yashe::encrypt and its samplers (src/yashe.cpp:104-142,
+ * src/distribution.cpp:4-60, src/cuda_distribution.cu:11-35). */
+cy_status cy_yashe_encrypt(cy_yashe *y, const uint64_t *d_m, uint64_t *d_ct, int batch, uint64_t seed,
+                           cy_stream_t stream);
+
+/* The CDT thresholds T_0 .. T_{2B} that cy_yashe_encrypt uses for width sigma
+ * (host only, no GPU). *n_entries is set to 2B+1; fails if it exceeds
+ * max_entries. No counterpart in the reference, whose sampler is cuRAND. */
+cy_status cy_gaussian_cdt(double sigma, uint64_t *out, int max_entries, int *n_entries);
+
 /* m = [round(t/q * [key*c]_q)]_t on the GPU for every coefficient; key = f, or
  * f^2 when `aftermul` (a product that was not relinearised). m: [batch][N]
  * uint64. Replaces Yashe::decrypt (src/yashe.cpp:143-201), which decrypts

@@ -144,6 +144,15 @@ class Yashe:
         dm = [(p.delta * (mv % p.t)) for mv in m]
         return [(hv + ev + dv) % p.q for hv, ev, dv in zip(hs, e, dm)]
 
+    def encrypt_with_errors(self, keys: YasheKeys, m: Sequence[int], s: Sequence[int],
+                            e: Sequence[int]) -> List[int]:
+        """[h*s + e + Delta*(m mod t)]_q for given error polynomials s, e
+        (the formula of encrypt above; the GPU encryption draws s and e with
+        the counter-based sampler of oracle/sampling.py)."""
+        p = self.p
+        hs = _mul_mod_q(keys.h, [int(v) for v in s], p.q, self._ntt)
+        return [(hv + int(ev) + p.delta * (int(mv) % p.t)) % p.q for hv, ev, mv in zip(hs, e, m)]
+
     def decrypt(self, keys: YasheKeys, c: Sequence[int], aftermul: bool = False) -> List[int]:
         p = self.p
         key = keys.f2 if aftermul else keys.f
