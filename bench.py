@@ -575,6 +575,24 @@ def run_ours(args):
     except Exception as e:  # reported, not fatal for the headline
         log("mixed batch failed:", e)
 
+    # ---- GPU encryption (on-device sampling) and decryption of the batch ---------
+    crypt = None
+    try:
+        MSG = torch.from_numpy(np.ascontiguousarray(m1[idx1]).view(np.int64)).cuda()
+        CT = Y.ring.empty(B)
+        Y.encrypt(MSG, seed=5, out=CT)
+        DEC = Y.decrypt(CT)
+        torch.cuda.synchronize()
+        enc_ok = torch.equal(DEC, MSG)
+        enc_ms = time_steps(lambda: Y.encrypt(MSG, seed=6, out=CT), max(3, args.steps // 4), stream)
+        dec_ms = time_steps(lambda: Y.decrypt(CT), max(3, args.steps // 4), stream)
+        reps = max(3, args.steps // 4)
+        crypt = {"encrypt_per_s": B * reps / (enc_ms / 1000.0), "decrypt_per_s": B * reps / (dec_ms / 1000.0),
+                 "batch": B, "decrypt_of_encrypt_ok": bool(enc_ok)}
+        log("encrypt/decrypt:", crypt)
+    except Exception as e:
+        log("encrypt bench failed:", e)
+
     # ---- deep level: N = 16384, 380-bit q, 64 pairs ------------------------------
     deep = None
     if not args.no_deep:
@@ -655,6 +673,7 @@ def run_ours(args):
         "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
                     "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
         "mixed_batch": mixed,
+        "gpu_encrypt_decrypt": crypt,
         "deep_level": deep,
         "cuda_graph": graphs,
         "serving": serving,

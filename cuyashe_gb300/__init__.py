@@ -80,6 +80,15 @@ class ServerStats(ctypes.Structure):
                 ("peak_device_bytes", ctypes.c_size_t)]
 
 
+class BlobInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("n", ctypes.c_int), ("q_limbs", ctypes.c_int), ("count", ctypes.c_int),
+                ("w_bits", ctypes.c_int), ("t", ctypes.c_uint64), ("q", ctypes.c_uint64 * 12),
+                ("bytes", ctypes.c_size_t)]
+
+
+BLOB_CIPHERTEXTS, BLOB_PUBLIC_KEY, BLOB_SECRET_KEY, BLOB_EVAL_KEY, BLOB_KEYS = 1, 2, 3, 4, 5
+
+
 class PolymulJob(ctypes.Structure):
     _fields_ = [("ring", ctypes.c_void_p), ("d_a", ctypes.c_void_p), ("d_b", ctypes.c_void_p),
                 ("d_c", ctypes.c_void_p)]
@@ -125,6 +134,12 @@ SIGNATURES = {
     "cy_yashe_mul_host": ([_vp, _vp, _vp, _vp, _i, _i], _i),
     "cy_yashe_encrypt": ([_vp, _vp, _vp, _i, ctypes.c_uint64, _vp], _i),
     "cy_gaussian_cdt": ([ctypes.c_double, _u64p, _i, ctypes.POINTER(_i)], _i),
+    "cy_serialize": ([ctypes.c_uint32, _i, _vp, _i, ctypes.c_uint64, _i, _vp, _i, _vp, ctypes.c_size_t,
+                      ctypes.POINTER(ctypes.c_size_t)], _i),
+    "cy_blob_info_read": ([_vp, ctypes.c_size_t, ctypes.POINTER(BlobInfo)], _i),
+    "cy_deserialize": ([_vp, ctypes.c_size_t, _vp, ctypes.c_size_t], _i),
+    "cy_yashe_save_keys": ([_vp, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], _i),
+    "cy_yashe_load_keys": ([_vp, _vp, ctypes.c_size_t], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
     "cy_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)], _i),

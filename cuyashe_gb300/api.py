@@ -19,7 +19,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from . import (CY_OK, PolymulJob, RingInfo, ServeRequest, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
+from . import (CY_OK, BLOB_KEYS, BlobInfo, PolymulJob, RingInfo, ServeRequest, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
                _stream_handle, check, lib, limbs_of)
 
 
@@ -54,6 +54,36 @@ def _host_ptr(x) -> int:
     if x.device.type != "cpu" or not x.is_contiguous() or x.element_size() != 8:
         raise ValueError("host tensors must be contiguous CPU tensors with 8-byte elements")
     return x.data_ptr()
+
+
+def serialize(kind: int, n: int, q: int, polys: np.ndarray, t: int = 0, w_bits: int = 0) -> bytes:
+    """Blob (cy_serialize) of polynomials [count][n][L] uint64 limbs mod q."""
+    L = nlimbs(q)
+    polys = np.ascontiguousarray(polys, dtype=np.uint64).reshape(-1, n, L)
+    qa = np.array([(q >> (64 * i)) & (2**64 - 1) for i in range(L)], dtype=np.uint64)
+    need = ctypes.c_size_t(0)
+    check(lib().cy_serialize(kind, n, qa.ctypes.data, L, t, w_bits, polys.ctypes.data, polys.shape[0], None, 0,
+                             ctypes.byref(need)), "cy_serialize")
+    buf = ctypes.create_string_buffer(need.value)
+    check(lib().cy_serialize(kind, n, qa.ctypes.data, L, t, w_bits, polys.ctypes.data, polys.shape[0], buf,
+                             need.value, ctypes.byref(need)), "cy_serialize")
+    return buf.raw
+
+
+def blob_info(blob: bytes) -> dict:
+    info = BlobInfo()
+    check(lib().cy_blob_info_read(blob, len(blob), ctypes.byref(info)), "cy_blob_info_read")
+    q = sum(int(info.q[i]) << (64 * i) for i in range(info.q_limbs))
+    return {"kind": info.kind, "n": info.n, "q": q, "q_limbs": info.q_limbs, "count": info.count, "t": info.t,
+            "w_bits": info.w_bits, "bytes": info.bytes}
+
+
+def deserialize(blob: bytes):
+    """(header dict, polynomials [count][n][L] uint64) of a checked blob."""
+    info = blob_info(blob)
+    out = np.zeros((info["count"], info["n"], info["q_limbs"]), np.uint64)
+    check(lib().cy_deserialize(blob, len(blob), out.ctypes.data, out.size), "cy_deserialize")
+    return info, out
 
 
 def to_device(arr: np.ndarray, device="cuda"):
@@ -259,6 +289,17 @@ class Yashe:
         H = to_limb_array(h, self.L) if not isinstance(h, np.ndarray) else np.ascontiguousarray(h, np.uint64)
         EV = to_limb_array(evk, self.L) if not isinstance(evk, np.ndarray) else np.ascontiguousarray(evk, np.uint64)
         check(lib().cy_yashe_set_keys(self.h, F.ctypes.data, H.ctypes.data, EV.ctypes.data), "cy_yashe_set_keys")
+
+    def save_keys(self) -> bytes:
+        """The installed keys as one blob (cy_yashe_save_keys)."""
+        need = ctypes.c_size_t(0)
+        check(lib().cy_yashe_save_keys(self.h, None, 0, ctypes.byref(need)), "cy_yashe_save_keys")
+        buf = ctypes.create_string_buffer(need.value)
+        check(lib().cy_yashe_save_keys(self.h, buf, need.value, ctypes.byref(need)), "cy_yashe_save_keys")
+        return buf.raw
+
+    def load_keys(self, blob: bytes) -> None:
+        check(lib().cy_yashe_load_keys(self.h, blob, len(blob)), "cy_yashe_load_keys")
 
     def get_keys(self):
         F = np.zeros((self.n, self.L), np.uint64)

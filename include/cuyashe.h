@@ -274,6 +274,45 @@ cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, 
                        cy_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Wire / on-disk format for keys and ciphertexts (host only, no GPU)         */
+/*                                                                            */
+/* The reference has no serialised form (keys and ciphertexts are NTL objects */
+/* in process memory). A blob is: magic "CYSH", u32 version (1), u32 kind,    */
+/* u32 n, u32 q_limbs L, u32 count, u64 t, u32 w_bits, u32 reserved, q as L   */
+/* u64, the polynomials [count][n][L] u64 (coefficients in [0, q)), and a u64 */
+/* FNV-1a checksum of every preceding byte; all little endian.                */
+
+#define CY_BLOB_CIPHERTEXTS 1u
+#define CY_BLOB_PUBLIC_KEY 2u
+#define CY_BLOB_SECRET_KEY 3u
+#define CY_BLOB_EVAL_KEY 4u
+#define CY_BLOB_KEYS 5u /* f, h, evk_0 .. evk_{ell-1} */
+#define CY_BLOB_MAX_LIMBS 12
+
+typedef struct cy_blob_info {
+    uint32_t kind;
+    int n, q_limbs, count, w_bits;
+    uint64_t t;
+    uint64_t q[CY_BLOB_MAX_LIMBS];
+    size_t bytes; /* total size of the blob */
+} cy_blob_info;
+
+/* Writes a blob of `count` polynomials into buf (len bytes); *needed gets its
+ * size. buf == NULL only reports the size. Rejects coefficients >= q. */
+cy_status cy_serialize(uint32_t kind, int n, const uint64_t *q, int q_limbs, uint64_t t, int w_bits,
+                       const uint64_t *polys, int count, void *buf, size_t len, size_t *needed);
+/* Reads and checks a blob's header and checksum. */
+cy_status cy_blob_info_read(const void *buf, size_t len, cy_blob_info *info);
+/* Copies a checked blob's polynomials (count*n*q_limbs words) to polys. */
+cy_status cy_deserialize(const void *buf, size_t len, uint64_t *polys, size_t max_words);
+
+/* The keys of a scheme as one CY_BLOB_KEYS blob, and back (the parameters in
+ * the blob must equal the scheme's). With a serving process these save its
+ * resident keys and resume with them. */
+cy_status cy_yashe_save_keys(const cy_yashe *y, void *buf, size_t len, size_t *needed);
+cy_status cy_yashe_load_keys(cy_yashe *y, const void *buf, size_t len);
+
+/* ------------------------------------------------------------------------ */
 /* Serving: continuous batching of HE multiplies                              */
 /* ------------------------------------------------------------------------ */
 
