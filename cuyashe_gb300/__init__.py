@@ -142,6 +142,8 @@ SIGNATURES = {
     "cy_yashe_load_keys": ([_vp, _vp, ctypes.c_size_t], _i),
     "cy_yashe_keyswitch": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_add": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_yashe_add_plain": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
+    "cy_yashe_mul_plain": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
     "cy_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)], _i),
     "cy_server_destroy": ([_vp], _i),
     "cy_server_register": ([_vp, _vp, ctypes.POINTER(_i)], _i),

@@ -360,6 +360,20 @@ class Yashe:
                                               ctypes.byref(h)), "cy_yashe_mul_graph_create")
         return Graph(h, (c1, c2, out, self))
 
+    def add_plain(self, c, m, out=None, stream=None):
+        """[c + Delta*(m mod t)]_q; m: [batch][N] device words."""
+        out = self.ring.empty(c.shape[0]) if out is None else out
+        check(lib().cy_yashe_add_plain(self.h, _ptr(c), _ptr(m), _ptr(out), c.shape[0], _stream_handle(stream)),
+              "cy_yashe_add_plain")
+        return out
+
+    def mul_plain(self, c, m, out=None, stream=None):
+        """[c * m_c]_q, m_c the centred representative of m mod t."""
+        out = self.ring.empty(c.shape[0]) if out is None else out
+        check(lib().cy_yashe_mul_plain(self.h, _ptr(c), _ptr(m), _ptr(out), c.shape[0], _stream_handle(stream)),
+              "cy_yashe_mul_plain")
+        return out
+
     def keyswitch(self, c, out=None, stream=None):
         out = self.ring.empty(c.shape[0]) if out is None else out
         check(lib().cy_yashe_keyswitch(self.h, _ptr(c), _ptr(out), c.shape[0], _stream_handle(stream)),

@@ -39,7 +39,7 @@ def sources():
 def headers():
     out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     inc = os.path.join(ROOT, "include")
-    out += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith((".h", ".hpp"))]
+    out += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]  # the .hpp is caller-side
     return out
 
 

@@ -175,9 +175,107 @@ __global__ void k_enc_finish(EncConsts C, const uint64_t* __restrict__ T, const 
     reduce_small_multiple(x, C.q, C.l64, c);
 }
 
+// out = [c + Delta*(m mod t)]_q (plaintext addition)
+__global__ void k_add_plain(EncConsts C, const uint64_t* __restrict__ m, const uint64_t* __restrict__ cin,
+                            uint64_t* __restrict__ out, int batch) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ((long long)batch << C.logn)) return;
+    const uint64_t mv = m[idx] % C.t;
+    const uint64_t* c = cin + idx * C.l64;
+    uint64_t x[7];
+    unsigned __int128 carry = 0;
+    for (int w = 0; w < C.l64; w++) {  // < Delta t + q <= 2q
+        const unsigned __int128 v = (unsigned __int128)C.delta[w] * mv + c[w] + carry;
+        x[w] = (uint64_t)v;
+        carry = v >> 64;
+    }
+    x[C.l64] = (uint64_t)carry;
+    reduce_small_multiple(x, C.q, C.l64, out + idx * C.l64);
+}
+
+// out = [m_c]_q with m_c the representative of m mod t in (-t/2, t/2]
+__global__ void k_lift_plain(EncConsts C, const uint64_t* __restrict__ m, uint64_t* __restrict__ out, int batch) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ((long long)batch << C.logn)) return;
+    const uint64_t v = m[idx] % C.t;
+    uint64_t* dst = out + idx * C.l64;
+    if (v <= C.t / 2) {
+        dst[0] = v;
+        for (int w = 1; w < C.l64; w++) dst[w] = 0;
+    } else {  // q - (t - v)
+        uint64_t borrow = C.t - v;
+        for (int w = 0; w < C.l64; w++) {
+            const unsigned __int128 d = (unsigned __int128)C.q[w] - borrow;
+            dst[w] = (uint64_t)d;
+            borrow = (d >> 64) ? 1 : 0;
+        }
+    }
+}
+
 }  // namespace cy
 
 using namespace cy;
+
+namespace {
+
+cy_status plain_consts(cy_yashe* y, EncConsts& C) {
+    cy_ring* r = y->ring;
+    int cur = -1;
+    CY_CUDA(cudaGetDevice(&cur));
+    if (cur != r->device) return set_error(CY_ERR_INVALID_ARGUMENT, "handle belongs to another CUDA device");
+    if (r->l64 > 6) return set_error(CY_ERR_UNSUPPORTED, "plaintext operations support q of up to 384 bits");
+    C = EncConsts{};
+    r->q.to_limbs64(C.q, r->l64);
+    (r->q / BigUInt(y->t)).to_limbs64(C.delta, r->l64);
+    C.t = (uint32_t)y->t;
+    C.l64 = r->l64;
+    C.logn = r->logn;
+    return CY_OK;
+}
+
+cy_status plain_args(cy_yashe* y, const void* a, const void* b, const void* out, int batch) {
+    if (!y) return set_error(CY_ERR_INVALID_ARGUMENT, "yashe handle is NULL");
+    if (batch < 0 || (batch > 0 && (!a || !b || !out))) return set_error(CY_ERR_INVALID_ARGUMENT, "bad argument");
+    for (const void* p : {a, out})
+        if (((uintptr_t)p & 15) != 0) return set_error(CY_ERR_INVALID_ARGUMENT, "buffer not 16-byte aligned");
+    return CY_OK;
+}
+
+}  // namespace
+
+extern "C" cy_status cy_yashe_add_plain(cy_yashe* y, const uint64_t* d_c, const uint64_t* d_m, uint64_t* d_out,
+                                        int batch, cy_stream_t stream) {
+    CY_TRY(plain_args(y, d_c, d_m, d_out, batch));
+    if (batch == 0) return CY_OK;
+    EncConsts C;
+    CY_TRY(plain_consts(y, C));
+    const long long total = (long long)batch << C.logn;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int tr = trace_begin("add_plain", C.logn, st);
+    k_add_plain<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, d_m, d_c, d_out, batch);
+    trace_end(tr, st);
+    CY_CUDA(cudaGetLastError());
+    return CY_OK;
+}
+
+extern "C" cy_status cy_yashe_mul_plain(cy_yashe* y, const uint64_t* d_c, const uint64_t* d_m, uint64_t* d_out,
+                                        int batch, cy_stream_t stream) {
+    CY_TRY(plain_args(y, d_c, d_m, d_out, batch));
+    if (batch == 0) return CY_OK;
+    if (d_out == d_c) return set_error(CY_ERR_INVALID_ARGUMENT, "out must not alias the ciphertext");
+    EncConsts C;
+    CY_TRY(plain_consts(y, C));
+    cy_ring* r = y->ring;
+    std::lock_guard<std::mutex> lock(r->mu);
+    const long long total = (long long)batch << C.logn;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int tr = trace_begin("lift_plain", C.logn, st);
+    k_lift_plain<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, d_m, d_out, batch);
+    trace_end(tr, st);
+    CY_CUDA(cudaGetLastError());
+    const long long stride = (long long)r->n * r->l64;
+    return run_product_api(r->mul, false, d_c, stride, d_out, stride, d_out, stride, batch, r->own_ws.ws, st);
+}
 
 extern "C" cy_status cy_gaussian_cdt(double sigma, uint64_t* out, int max_entries, int* n_entries) {
     if (!(sigma > 0.0) || !n_entries || max_entries < 0 || (max_entries > 0 && !out))

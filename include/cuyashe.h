@@ -269,6 +269,18 @@ cy_status cy_yashe_mul_host(cy_yashe *y, const uint64_t *h_c1, const uint64_t *h
 /* Relinearisation alone: out = [sum_d D_d(c)*evk_d]_q (Ciphertext::convert). */
 cy_status cy_yashe_keyswitch(cy_yashe *y, const uint64_t *d_c, uint64_t *d_out, int batch, cy_stream_t stream);
 
+/* Plaintext operations. add_plain: out = [c + Delta*(m mod t)]_q, the scheme's
+ * addition of a plaintext (the reference's Ciphertext::operator+(Polynomial),
+ * src/ciphertext.cpp:11-15, adds a polynomial that the caller has already
+ * scaled; cy_polyadd does that). mul_plain: out = [c * m_c]_q with m_c the
+ * representative of m mod t in (-t/2, t/2], which decrypts to the product of
+ * the plaintexts mod t; no counterpart in the reference. d_m: [batch][N]
+ * uint64; out must not alias c for mul_plain. Asynchronous on `stream`. */
+cy_status cy_yashe_add_plain(cy_yashe *y, const uint64_t *d_c, const uint64_t *d_m, uint64_t *d_out, int batch,
+                             cy_stream_t stream);
+cy_status cy_yashe_mul_plain(cy_yashe *y, const uint64_t *d_c, const uint64_t *d_m, uint64_t *d_out, int batch,
+                             cy_stream_t stream);
+
 /* Homomorphic add (Ciphertext::operator+, src/ciphertext.cpp:4-23). */
 cy_status cy_yashe_add(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out, int batch,
                        cy_stream_t stream);

@@ -11,7 +11,8 @@
 //               reduce (kept for compatibility; results are already reduced);
 //   Ciphertext: operator* (tensor product, marked `aftermul` as in the
 //               reference, relinearised lazily), convert (keyswitch), +;
-//   Yashe:      generate_keys, encrypt, decrypt.
+//   Yashe:      generate_keys, encrypt (on the GPU), decrypt; Ciphertext + and *
+//               by a plaintext polynomial.
 // Differences: the statics become a Context (the ring) and a Yashe object;
 // coefficients are cuyashe::ZZ (a host big integer, NTL is not needed); every
 // product runs on the GPU through cy_polymul / cy_yashe_mul; errors throw
@@ -76,6 +77,26 @@ class Context {
     int n_;
     ZZ q_;
     int limbs_;
+};
+
+// A device copy of host words (owned, freed on destruction).
+class DeviceWords {
+   public:
+    explicit DeviceWords(const std::vector<uint64_t>& h) : n_(h.size()) {
+        check_cuda(cudaMalloc(&d_, n_ * sizeof(uint64_t)), "cudaMalloc");
+        check_cuda(cudaMemcpy(d_, h.data(), n_ * sizeof(uint64_t), cudaMemcpyHostToDevice), "H2D");
+    }
+    DeviceWords(DeviceWords&& o) noexcept : d_(o.d_), n_(o.n_) { o.d_ = nullptr; }
+    DeviceWords(const DeviceWords&) = delete;
+    DeviceWords& operator=(const DeviceWords&) = delete;
+    ~DeviceWords() {
+        if (d_) cudaFree(d_);
+    }
+    const uint64_t* get() const { return d_; }
+
+   private:
+    uint64_t* d_ = nullptr;
+    size_t n_;
 };
 
 class Polynomial {
@@ -285,6 +306,9 @@ class Ciphertext : public Polynomial {
     Ciphertext(Yashe& y);
     Ciphertext operator*(Ciphertext& b);
     Ciphertext operator+(Ciphertext& b);
+    // plaintext operand m in R_t: c + Delta*m, and c * m (m centred mod t)
+    Ciphertext operator+(const Polynomial& m);
+    Ciphertext operator*(const Polynomial& m);
     void convert();
     int level = 0;
     bool aftermul = false;
@@ -323,19 +347,19 @@ class Yashe {
 
     void generate_keys(uint64_t seed = 1234) { check(cy_yashe_keygen(y_, seed), "cy_yashe_keygen"); }
 
-    // c = [Delta*m + e + h*s]_q; m in R_t (src/yashe.cpp:104-142)
-    Ciphertext encrypt(const Polynomial& m, uint64_t seed = 1) {
+    // c = [Delta*m + e + h*s]_q with s, e drawn on the GPU; m in R_t
+    // (src/yashe.cpp:104-142)
+    Ciphertext encrypt(const Polynomial& m, uint64_t seed = 1);
+
+    // plaintext coefficients as one word each, on the device
+    DeviceWords plaintext_words(const Polynomial& m) const {
         std::vector<uint64_t> mv(n_);
         for (int i = 0; i < n_; i++) {
             const ZZ v = m.get_coeff(i);
-            if (v >= ZZ(t_)) throw Error(CY_ERR_INVALID_ARGUMENT, "Yashe::encrypt: plaintext coefficient >= t");
+            if (v >= ZZ(t_)) throw Error(CY_ERR_INVALID_ARGUMENT, "plaintext coefficient >= t");
             mv[i] = v.low64();
         }
-        Ciphertext c(*this);
-        std::vector<uint64_t> ct((size_t)n_ * ctx_->limbs());
-        check(cy_yashe_encrypt_host(y_, mv.data(), ct.data(), 1, seed), "cy_yashe_encrypt_host");
-        c.set_limbs(ct.data());
-        return c;
+        return DeviceWords(mv);
     }
 
     // m = [round(t/q [key*c]_q)]_t for every coefficient (src/yashe.cpp:143-201)
@@ -361,6 +385,36 @@ class Yashe {
 };
 
 inline Ciphertext::Ciphertext(Yashe& y) : Polynomial(y.context()), y_(&y) {}
+
+inline Ciphertext Yashe::encrypt(const Polynomial& m, uint64_t seed) {
+    const DeviceWords dm = plaintext_words(m);
+    Ciphertext c(*this);
+    check(cy_yashe_encrypt(y_, dm.get(), c.mutable_device(), 1, seed, nullptr), "cy_yashe_encrypt");
+    c.dev_written();
+    return c;
+}
+
+inline Ciphertext Ciphertext::operator+(const Polynomial& m) {
+    const DeviceWords dm = y_->plaintext_words(m);
+    Ciphertext c(*y_);
+    check(cy_yashe_add_plain(y_->handle(), device_data(), dm.get(), c.mutable_device(), 1, nullptr),
+          "cy_yashe_add_plain");
+    c.dev_written();
+    c.level = level;
+    c.aftermul = aftermul;
+    return c;
+}
+
+inline Ciphertext Ciphertext::operator*(const Polynomial& m) {
+    const DeviceWords dm = y_->plaintext_words(m);
+    Ciphertext c(*y_);
+    check(cy_yashe_mul_plain(y_->handle(), device_data(), dm.get(), c.mutable_device(), 1, nullptr),
+          "cy_yashe_mul_plain");
+    c.dev_written();
+    c.level = level;
+    c.aftermul = aftermul;
+    return c;
+}
 
 inline Ciphertext Ciphertext::operator*(Ciphertext& b) {
     if (b.y_ != y_) throw Error(CY_ERR_INVALID_ARGUMENT, "ciphertexts of different schemes");

@@ -153,6 +153,17 @@ class Yashe:
         hs = _mul_mod_q(keys.h, [int(v) for v in s], p.q, self._ntt)
         return [(hv + int(ev) + p.delta * (int(mv) % p.t)) % p.q for hv, ev, mv in zip(hs, e, m)]
 
+    def add_plain(self, c: Sequence[int], m: Sequence[int]) -> List[int]:
+        """[c + Delta*(m mod t)]_q (a plaintext added to a ciphertext)."""
+        p = self.p
+        return [(int(cv) + p.delta * (int(mv) % p.t)) % p.q for cv, mv in zip(c, m)]
+
+    def mul_plain(self, c: Sequence[int], m: Sequence[int]) -> List[int]:
+        """[c * m_c]_q with m_c the representative of m mod t in (-t/2, t/2]."""
+        p = self.p
+        mc = [(int(mv) % p.t) - (p.t if (int(mv) % p.t) > p.t // 2 else 0) for mv in m]
+        return _mul_mod_q(list(c), mc, p.q, self._ntt)
+
     def decrypt(self, keys: YasheKeys, c: Sequence[int], aftermul: bool = False) -> List[int]:
         p = self.p
         key = keys.f2 if aftermul else keys.f

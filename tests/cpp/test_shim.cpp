@@ -256,6 +256,16 @@ void yashe_case(const char* suite, int n, const ZZ& q, uint64_t t, uint64_t seed
         REQUIRE(c.level == 2);
         REQUIRE(cipher.decrypt(c) == (a * b) * d);
     });
+    run(name("encryptandAddPlain").c_str(), [&] {
+        Polynomial a = plain(), b = plain();
+        Ciphertext c = cipher.encrypt(a, rng.next());
+        REQUIRE(cipher.decrypt(c + b) == (a + b));
+    });
+    run(name("encryptandMulPlain").c_str(), [&] {
+        Polynomial a = plain(), b = plain();
+        Ciphertext c = cipher.encrypt(a, rng.next());
+        REQUIRE(cipher.decrypt(c * b) == (a * b));
+    });
     run(name("encryptRejectsLargeCoefficients").c_str(), [&] {
         Polynomial a(cipher.context());
         a.set_coeff(0, ZZ(t));

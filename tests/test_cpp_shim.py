@@ -50,4 +50,4 @@ def test_cpp_api_reference_suites(tmp_path):
     res = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stdout + res.stderr
     lines = [l for l in res.stdout.splitlines() if l.startswith(("ok", "FAIL"))]
-    assert len(lines) >= 19 and all(l.startswith("ok") for l in lines), res.stdout
+    assert len(lines) >= 23 and all(l.startswith("ok") for l in lines), res.stdout

@@ -30,10 +30,6 @@ def cy():
     return cuyashe_gb300
 
 
-def _words(vals, L):
-    return [[(v >> (64 * w)) & (2**64 - 1) for w in range(L)] for v in vals]
-
-
 @pytest.mark.parametrize("n,qbits,t", [(64, 127, 257), (256, 62, 65537), (1024, 190, 1024)])
 def test_encrypt_matches_oracle(cy, n, qbits, t):
     import torch
@@ -112,3 +108,50 @@ def test_encrypt_rejects_bad_arguments(cy):
     assert lib.cy_yashe_encrypt(Y.h, 0, ct.data_ptr(), 1, 1, None) == -1
     assert lib.cy_yashe_encrypt(Y.h, m.data_ptr(), ct.data_ptr() + 8, 1, 1, None) == -1  # misaligned
     assert lib.cy_yashe_encrypt(None, m.data_ptr(), ct.data_ptr(), 1, 1, None) == -1
+
+
+@pytest.mark.parametrize("n,qbits,t", [(64, 127, 257), (256, 190, 65537)])
+def test_plaintext_ops_match_oracle(cy, n, qbits, t):
+    import torch
+
+    q = ring.largest_prime_below(2**qbits, congruent_mod=2 * n)
+    oy = OYashe(YasheParams(n=n, q=q, t=t, w_bits=32))
+    keys = oy.keygen(n + 11)
+    Y = cy.Yashe(n, q, t)
+    Y.set_keys(keys.f, keys.h, keys.evk)
+    rng = random.Random(n + 1)
+    m1 = [[rng.randrange(t) for _ in range(n)] for _ in range(2)]
+    m2 = [[rng.randrange(2 * t) for _ in range(n)] for _ in range(2)]  # taken mod t
+    cts = [oy.encrypt(keys, m, 50 + i) for i, m in enumerate(m1)]
+    C = Y.ring.upload(cts)
+    M2 = torch.tensor(np.array(m2, dtype=np.uint64).view(np.int64), device="cuda")
+    add = Y.ring.download(Y.add_plain(C, M2))
+    mul = Y.ring.download(Y.mul_plain(C, M2))
+    for j in range(2):
+        assert list(add[j]) == oy.add_plain(cts[j], m2[j])
+        assert list(mul[j]) == oy.mul_plain(cts[j], m2[j])
+        m2t = [v % t for v in m2[j]]
+        assert oy.decrypt(keys, list(add[j])) == [(a + b) % t for a, b in zip(m1[j], m2t)]
+        assert oy.decrypt(keys, list(mul[j])) == ring.polymul_mod(m1[j], m2t, t)
+
+
+def test_plaintext_ops_decrypt_at_full_size(cy):
+    import torch
+
+    n, t, batch = 4096, 1024, 16
+    Y = cy.Yashe(n, QY, t)
+    Y.keygen(12)
+    rng = np.random.default_rng(6)
+    m1 = rng.integers(0, t, size=(batch, n), dtype=np.uint64)
+    m2 = rng.integers(0, t, size=(batch, n), dtype=np.uint64)
+    d1 = torch.from_numpy(m1.view(np.int64)).cuda()
+    d2 = torch.from_numpy(m2.view(np.int64)).cuda()
+    c = Y.encrypt(d1, seed=21)
+    got_add = Y.decrypt(Y.add_plain(c, d2)).cpu().numpy().view(np.uint64)
+    assert np.array_equal(got_add, (m1 + m2) % t)
+    got_mul = Y.decrypt(Y.mul_plain(c, d2)).cpu().numpy().view(np.uint64)
+    PT = cy.Ring(n, t)
+    want = PT.polymul(PT.upload(m1[:2].astype(object).tolist()), PT.upload(m2[:2].astype(object).tolist()))
+    assert np.array_equal(got_mul[:2], want.cpu().numpy().view(np.uint64)[..., 0])
+    lib = cy.lib()
+    assert lib.cy_yashe_mul_plain(Y.h, c.data_ptr(), d2.data_ptr(), c.data_ptr(), batch, None) == -1  # aliasing
