@@ -20,6 +20,10 @@ void fill_n12_e3r(KernelSet& ks);
 void fill_n12_e4r(KernelSet& ks);
 void fill_n13_e4r(KernelSet& ks);
 void fill_n14_e5(KernelSet& ks);
+void fill_n12_e4s(KernelSet& ks);
+void fill_n12_e3s(KernelSet& ks);
+void fill_n12_e4m(KernelSet& ks);
+void fill_n13_e4s(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -52,6 +56,10 @@ static const VariantTable& variants() {
         add(12, fill_n12_e4r);
         add(13, fill_n13_e4r);
         add(14, fill_n14_e5);
+        add(12, fill_n12_e4s);  // one keyswitch exchange region: two blocks per SM
+        add(12, fill_n12_e3s);
+        add(12, fill_n12_e4m);
+        add(13, fill_n13_e4s);
     });
     return T;
 }

@@ -161,7 +161,9 @@ constexpr int ks_min_blocks() {
 
 // MINB > 0 overrides the blocks per SM the kernel is compiled for (a schedule
 // with a larger register budget per thread).
-template <int LOGN, int LOGE, int L64, bool CENTER, int MINB = 0>
+// SINGLE: one exchange region (two barriers per exchange), so that more blocks
+// fit in shared memory.
+template <int LOGN, int LOGE, int L64, bool CENTER, int MINB = 0, bool SINGLE = false>
 __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul_min_blocks<LOGN, LOGE>()))
     k_mul(const BasisDev* __restrict__ B, const uint64_t* __restrict__ A, long long a_stride,
           const uint64_t* __restrict__ Bv, long long b_stride, uint32_t* __restrict__ resid) {
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
             x[1][e] = crt_coef<CENTER>(b, pos, l64, s_crt, s_qhalf, c);
         }
     }
-    constexpr int STRIDE = region_stride<PL, 2>();
+    constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, 2>();
     int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0);
     uint32_t z[1][E];
 #pragma unroll
@@ -227,7 +229,9 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
 // coefficients of c in [0, q) (w = 2^32), processed ND at a time.
 // evk: [ell][k][N] (value, Shoup companion) in the forward-NTT output order.
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, int L64, int ND, int MINB = 0>
+// SINGLE: one exchange region (two barriers per exchange) instead of two, so
+// that more blocks fit in shared memory.
+template <int LOGN, int LOGE, int L64, int ND, int MINB = 0, bool SINGLE = false>
 __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_min_blocks<LOGN, LOGE>()))
     k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
                 int ell, uint32_t* __restrict__ resid) {
@@ -243,7 +247,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
     const uint64_t* cj = C + (size_t)job * PL::N * l64;
-    constexpr int STRIDE = region_stride<PL, ND>();
+    constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, ND>();
 
     uint32_t acc[1][E];
 #pragma unroll
@@ -589,36 +593,38 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
 
 namespace cy {
 
-template <int LOGN, int LOGE, int L64, int MB_MUL, int MB_KS>
+template <int LOGN, int LOGE, int L64, int MB_MUL, int MB_KS, bool SINGLE_KS, bool SINGLE_MUL>
 void fill_l64(KernelSet& ks) {
-    ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false, MB_MUL>;
-    ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true, MB_MUL>;
-    ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, 2, MB_KS>;
-    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4, MB_KS>;
+    ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false, MB_MUL, SINGLE_MUL>;
+    ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true, MB_MUL, SINGLE_MUL>;
+    ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, 2, MB_KS, SINGLE_KS>;
+    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4, MB_KS, SINGLE_KS>;
 }
 
 // SPECIALISE: also instantiate the kernels for 1, 2, 3 and 6 limbs (q of up to
 // 64, 128, 192 and 384 bits); other limb counts use the generic kernels.
 // MB_MUL / MB_KS > 0: blocks per SM the product / keyswitch kernels are
 // compiled for (0: the defaults above).
-template <int LOGN, int LOGE, bool SPECIALISE, int MB_MUL = 0, int MB_KS = 0>
+// SINGLE_KS / SINGLE_MUL: the keyswitch / product kernels use one exchange region.
+template <int LOGN, int LOGE, bool SPECIALISE, int MB_MUL = 0, int MB_KS = 0, bool SINGLE_KS = false,
+          bool SINGLE_MUL = false>
 void fill_kernel_set(KernelSet& ks) {
     using PL = NttPlan<LOGN, LOGE>;
     ks.logn = LOGN;
     ks.loge = LOGE;
     ks.threads = PL::G;
-    fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS>(ks);
+    fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL>(ks);
     if constexpr (SPECIALISE) {
-        fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS>(ks);
-        fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS>(ks);
-        fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS>(ks);
-        fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS>(ks);
+        fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL>(ks);
+        fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL>(ks);
+        fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL>(ks);
+        fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL>(ks);
     }
     ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
     ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
-    ks.smem_mul = region_bytes<PL, 2>();
-    ks.smem_ks[0] = region_bytes<PL, 2>();
-    ks.smem_ks[1] = region_bytes<PL, 4>();
+    ks.smem_mul = SINGLE_MUL ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
+    ks.smem_ks[0] = SINGLE_KS ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
+    ks.smem_ks[1] = SINGLE_KS ? (size_t)4 * PL::SMW * 4 : region_bytes<PL, 4>();
     ks.smem_ntt = region_bytes<PL, 1>();
 }
 
