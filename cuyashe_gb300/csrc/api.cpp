@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -72,6 +73,11 @@ static cy_status launch(void* func, const char* name, int logn, dim3 grid, dim3 
     return CY_OK;
 }
 
+// Fixed-point YASHE rounding: coefficients whose estimate has a fraction at or
+// above this limit take the exact path (0: every coefficient does).
+static std::atomic<int> g_epi_exact{0};
+unsigned long long epi_frac_limit() { return g_epi_exact.load() ? 0ull : 0xFFFFFFF000000000ull; }
+
 static const char* epi_name(int mode) {
     return mode == EPI_YASHE ? "epi_yashe" : mode == EPI_DECRYPT ? "epi_decrypt" : "epi_modq";
 }
@@ -110,7 +116,8 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
         CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
                       dim3(ks.threads), ks.smem_mul, st, args));
         void* oj = (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t);
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        unsigned long long fl = epi_frac_limit();
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
         CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
                       dim3(kEpiThreads), 0, st, eargs));
@@ -141,7 +148,8 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
         CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel],
                       st, args));
         uint64_t* oj = out + (size_t)j0 * n * l64;
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        unsigned long long fl = epi_frac_limit();
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
         CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
                       dim3(kEpiThreads), 0, st, eargs));
@@ -409,12 +417,18 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
         const BasisDev* Bd = B.d;
         uint32_t* resid = ws.d_resid;
         uint64_t* oj = d_c + (size_t)j0 * n * r->l64;
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj};
+        unsigned long long fl = epi_frac_limit();
+        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
         CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
                       dim3(kEpiThreads), 0, st, eargs));
     }
     // the scale vector is read by the kernels above before the stream moves on
+    return CY_OK;
+}
+
+cy_status cy_set_epilogue_exact(int on) {
+    g_epi_exact.store(on ? 1 : 0);
     return CY_OK;
 }
 
@@ -464,7 +478,8 @@ cy_status cy_icrt(cy_ring* r, const uint32_t* d_res, uint64_t* d_x, int batch, c
         int nj = std::min(65536, batch - j0);
         const uint32_t* rj = d_res + (size_t)j0 * B.h.k * r->n;
         uint64_t* xj = d_x + (size_t)j0 * r->n * r->l64;
-        void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj};
+        unsigned long long fl = epi_frac_limit();
+        void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * r->n;
         CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
                       dim3(kEpiThreads), 0, (cudaStream_t)stream, eargs));

@@ -47,6 +47,8 @@ struct BasisDev {
     uint32_t crt[KMAX][L32MAX];        // 2^(32 j) mod p_i
     uint32_t A0[KMAX][L32MAX];  // MODQ: (Mhat_i mod q) << s     YASHE: (I_i mod q) << s, t*Mhat_i = I_i q + R_i
     uint32_t A1[KMAX][L32MAX];  //                                YASHE: R_i << s
+    uint32_t frac[KMAX][2];     // YASHE: floor(R_i 2^64 / q) (lo, hi words)
+    uint32_t frac_m[2];         // YASHE: floor((q - R_M) 2^64 / q)
     const uint2* psi[KMAX];     // forward twiddles (w, floor(w 2^32/p)), bit-reversed powers of psi
     const uint2* ipsi[KMAX];    // inverse twiddles
 };

@@ -453,6 +453,7 @@ struct EpiShared {
     uint32_t p[KPAD], ycon[KPAD], ycon_sh[KPAD], flo[KPAD], fhi[KPAD];
     uint32_t A0[KPAD * L32MAX];
     uint32_t A1[KPAD * L32MAX];
+    uint32_t F[KPAD * 2], FM[2];  // YASHE: R_i / q and (q - R_M) / q in units of 2^-64
     uint32_t B0[L32MAX], B1[L32MAX], qn[L32MAX], qhalf_n[L32MAX];
 };
 
@@ -474,6 +475,10 @@ __device__ __forceinline__ void epi_stage(EpiShared& S, const BasisDev* __restri
         S.A0[i] = in ? B->A0[i / L][i % L] : 0u;
         if (MODE == EPI_YASHE) S.A1[i] = in ? B->A1[i / L][i % L] : 0u;
     }
+    if (MODE == EPI_YASHE) {
+        for (int i = tid; i < kp * 2; i += nthreads) S.F[i] = i < k * 2 ? B->frac[i / 2][i % 2] : 0u;
+        if (tid < 2) S.FM[tid] = B->frac_m[tid];
+    }
     for (int i = tid; i < L; i += nthreads) {
         S.B0[i] = B->B0[i];
         S.B1[i] = B->B1[i];
@@ -482,27 +487,60 @@ __device__ __forceinline__ void epi_stage(EpiShared& S, const BasisDev* __restri
     }
 }
 
+// YASHE rounding, exact: Q = floor((S' + (q-1)/2) / q) with S' = sum y_i R_i +
+// v (q - R_M), from the residues again (the rare case that the fixed-point
+// estimate cannot decide).
+template <int L>
+__device__ __noinline__ uint64_t yashe_round_exact(const EpiShared& S, const BasisDev* __restrict__ B,
+                                                   const uint32_t* __restrict__ r0, size_t stride, uint32_t v) {
+    const int k = B->k;
+    Cols<L> c1;
+    c1.zero();
+    for (int i = 0; i < k; i++) {
+        const uint32_t p = S.p[i];
+        const uint32_t y = red(shoup(__ldcg(r0 + (size_t)i * stride), S.ycon[i], S.ycon_sh[i], p), p);
+        c1.mac(y, &S.A1[i * L]);
+        if (i % 3 == 2) c1.norm();
+    }
+    c1.norm();
+    c1.mac(v, S.B1);
+    c1.add(S.qhalf_n);
+    c1.norm();
+    uint32_t rdummy[L];
+    return barrett<L>(c1, S.qn, B->mu, rdummy);
+}
+
 // Epilogue of one coefficient: r0 points at its residue for prime 0, residues of
 // the next primes follow `stride` words apart. Writes limb j of `dst` (MODQ,
 // YASHE) or one word (DECRYPT).
+//
+// YASHE rounding: Q = round(S'/q) is first estimated in 64-bit fixed point,
+// Z = sum y_i F_i + v F_M + 2^63 (F = floor(R 2^64 / q)), which undershoots the
+// true value by less than (k+1) 2^30 2^-64 < 2^-28. floor(Z / 2^64) is exact
+// unless the fraction of Z is within 2^-28 of the next integer; those
+// coefficients (about one in 2^28), and all of them when frac_limit is 0, take
+// the exact multiword path.
 template <int L, int MODE>
 __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __restrict__ B,
-                                         const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst) {
+                                         const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst,
+                                         uint64_t frac_limit = 0) {
     const int k = B->k, shift = B->shift, l64 = B->l64;
     const int groups = (k + 2) / 3;
     const uint64_t mu = B->mu;
-    Cols<L> c0, c1;
+    Cols<L> c0;
+    Cols<2> fz;  // YASHE: Z in 32-bit columns
     c0.zero();
-    c1.zero();
+    fz.zero();
     uint64_t vacc = 0;
     // One prime's contribution: y = [X Mhat_i^-1]_{p_i}, the fixed-point estimate
-    // of y/p_i for v, and y times the row(s) of constants into the columns.
+    // of y/p_i for v, y times the row of constants into the columns and (YASHE)
+    // y F_i into Z.
     auto absorb = [&](int i, uint32_t r) {
         const uint32_t p = S.p[i];
         const uint32_t y = red(shoup(r, S.ycon[i], S.ycon_sh[i], p), p);
         vacc += (uint64_t)y * S.fhi[i] + __umulhi(y, S.flo[i]);  // sum y_i/p_i in 2^-32 units
         c0.mac(y, &S.A0[i * L]);
-        if (MODE == EPI_YASHE) c1.mac(y, &S.A1[i * L]);
+        if (MODE == EPI_YASHE) fz.mac(y, &S.F[i * 2]);
     };
     // Residues come from L2: the loads of the next two groups of three primes are
     // in flight while a group is absorbed. Loads past the last prime re-read its
@@ -519,7 +557,7 @@ __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __r
 #pragma unroll
         for (int j = 0; j < 3; j++) absorb(3 * g + j, g0[j]);
         c0.norm();  // columns take three products of < 2^62 between carry passes
-        if (MODE == EPI_YASHE) c1.norm();
+        if (MODE == EPI_YASHE) fz.norm();
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             g0[j] = g1[j];
@@ -530,12 +568,12 @@ __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __r
     c0.norm();
     c0.mac(v, S.B0);
     if (MODE == EPI_YASHE) {
-        c1.norm();
-        c1.mac(v, S.B1);
-        c1.add(S.qhalf_n);
-        c1.norm();
-        uint32_t rdummy[L];
-        const uint64_t Q2 = barrett<L>(c1, S.qn, mu, rdummy);  // round(S/q) + v, S = sum y_i R_i - v R_M
+        fz.mac(v, S.FM);
+        fz.c[1] += 0x80000000u;  // + 1/2
+        fz.norm();
+        const uint64_t frac = fz.c[0] | (fz.c[1] << 32);
+        uint64_t Q2 = fz.c[2] | (fz.c[3] << 32);  // round(S/q) + v, S = sum y_i R_i - v R_M
+        if (frac >= frac_limit) Q2 = yashe_round_exact<L>(S, B, r0, stride, v);
         // c0 += Q2 << shift
         const uint64_t lo = Q2 << shift;
         const uint64_t hi = shift ? (Q2 >> (64 - shift)) : 0;
@@ -574,7 +612,7 @@ __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __r
 
 template <int L, int MODE>
 __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
-                                             void* __restrict__ out, int njobs) {
+                                             void* __restrict__ out, int njobs, unsigned long long frac_limit) {
     __shared__ EpiShared S;
     epi_stage<L, MODE>(S, B, threadIdx.x, blockDim.x);
     __syncthreads();
@@ -586,7 +624,7 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
     const int coef = (int)(idx & (n - 1));
     uint64_t* dst = reinterpret_cast<uint64_t*>(out) +
                     (MODE == EPI_DECRYPT ? (size_t)job * n + coef : ((size_t)job * n + coef) * l64);
-    epi_coef<L, MODE>(S, B, resid + (size_t)job * k * n + coef, (size_t)n, dst);
+    epi_coef<L, MODE>(S, B, resid + (size_t)job * k * n + coef, (size_t)n, dst, frac_limit);
 }
 
 }  // namespace cy

@@ -98,7 +98,8 @@ extern "C" cy_status cy_polymul_noalloc(cy_ring* r, const uint64_t* d_a, const u
     CY_TRY(launch_noalloc(ks.mul_for(B.h.l64, false), "mul_noalloc", B.h.logn, dim3(k, batch), dim3(ks.threads),
                           ks.smem_mul, st, args));
     void* epi = epi_kernel(B.h.l32, EPI_MODQ);
-    void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch};
+    unsigned long long fl = 0;  // mod-q epilogue: no rounding estimate
+    void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch, (void*)&fl};
     const long long threads = (long long)batch * n;
     return launch_noalloc(epi, "epi_modq_noalloc", B.h.logn, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st,
                           eargs);

@@ -189,6 +189,7 @@ cy_status basis_constants(BasisDev& h, int* crt_bits, int n, const BigUInt& q, i
         BigUInt b0 = im1.is_zero() ? BigUInt() : q - im1;
         b0.shl(h.shift).to_words32(h.B0, L32MAX);
         (q - RM).shl(h.shift).to_words32(h.B1, L32MAX);
+        ((q - RM).shl(64) / q).to_words32(h.frac_m, 2);
     } else {
         BigUInt b0 = Mq.is_zero() ? BigUInt() : q - Mq;
         b0.shl(h.shift).to_words32(h.B0, L32MAX);
@@ -224,6 +225,7 @@ cy_status basis_constants(BasisDev& h, int* crt_bits, int n, const BigUInt& q, i
             BigUInt::divmod(Mhat * BigUInt(t), q, &I, &R);
             (I % q).shl(h.shift).to_words32(h.A0[i], L32MAX);
             R.shl(h.shift).to_words32(h.A1[i], L32MAX);
+            (R.shl(64) / q).to_words32(h.frac[i], 2);
         } else {
             (Mhat % q).shl(h.shift).to_words32(h.A0[i], L32MAX);
         }

@@ -246,6 +246,13 @@ cy_status cy_gaussian_cdt(double sigma, uint64_t *out, int max_entries, int *n_e
 cy_status cy_yashe_decrypt(cy_yashe *y, const uint64_t *d_ct, uint64_t *d_m, int batch, int aftermul,
                            cy_stream_t stream);
 
+/* The YASHE rounding round(t/q * x) is first estimated in 64-bit fixed point
+ * and computed exactly only for the rare coefficients (about one in 2^28) the
+ * estimate cannot decide; both give the same result. on != 0 makes every
+ * coefficient take the exact path (a check of the estimate; slower). Applies
+ * to calls made after it, process-wide. No counterpart in the reference. */
+cy_status cy_set_epilogue_exact(int on);
+
 /* Homomorphic multiply: out = [round(t/q * c1*c2)]_q with the product over
  * Z[x]/(x^N+1) on symmetric representatives, then (relin != 0) the keyswitch
  * [sum_d D_d(out)*evk_d]_q. Replaces Ciphertext::operator* and

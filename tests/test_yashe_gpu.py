@@ -192,3 +192,45 @@ def test_mul_without_keys_is_rejected(cy):
         Y.mul(z, z, relin=True)
     assert ei.value.status == -6
     Y.mul(z, z, relin=False)  # the tensor alone needs no key
+
+
+@pytest.mark.parametrize("n,q,t", [(64, Q127, 1024), (512, Q190, 65537), (64, Q380, 65537)])
+def test_fixed_point_rounding_equals_exact_path(cy, n, q, t):
+    """The tensor epilogue estimates round(t/q x) in fixed point and falls back
+    to the exact multiword path when undecided; forcing the exact path
+    everywhere must give the same ciphertexts, both equal to the oracle's."""
+    oy, keys, pts, cts = _setup(n, q, t)
+    Y = cy.Yashe(n, q, t)
+    Y.set_keys(keys.f, keys.h, keys.evk)
+    R = Y.ring
+    A, B = R.upload([cts[0], cts[1]]), R.upload([cts[2], cts[3]])
+    fast = R.download(Y.mul(A, B, relin=False))
+    lib = cy.lib()
+    lib.cy_set_epilogue_exact(1)
+    try:
+        exact = R.download(Y.mul(A, B, relin=False))
+    finally:
+        lib.cy_set_epilogue_exact(0)
+    assert [list(x) for x in fast] == [list(x) for x in exact]
+    for j in range(2):
+        assert list(fast[j]) == oy.mul_tensor(cts[j], cts[2 + j])
+
+
+def test_fixed_point_rounding_at_full_size(cy):
+    import torch
+
+    n, t = 4096, 1024
+    Y = cy.Yashe(n, Q127, t)
+    Y.keygen(17)
+    rng = np.random.default_rng(17)
+    m = torch.from_numpy(rng.integers(0, t, size=(256, n), dtype=np.uint64).view(np.int64)).cuda()
+    c1, c2 = Y.encrypt(m, seed=1), Y.encrypt(m.flip(0).contiguous(), seed=2)
+    fast = Y.mul(c1, c2, relin=False)
+    lib = cy.lib()
+    lib.cy_set_epilogue_exact(1)
+    try:
+        exact = Y.mul(c1, c2, relin=False)
+    finally:
+        lib.cy_set_epilogue_exact(0)
+    torch.cuda.synchronize()
+    assert torch.equal(fast, exact)
