@@ -28,6 +28,11 @@ void* crt_kernel();
 void* shoup_pairs_kernel();
 
 static constexpr int kEpiThreads = 256;
+// blocks of the epilogue kernel for `coefs` coefficients of a q of l32 words
+static unsigned epi_blocks(long long coefs, int l32) {
+    const long long per = (long long)kEpiThreads * epi_coefs_per_thread(l32);
+    return (unsigned)((coefs + per - 1) / per);
+}
 
 int trace_begin(const char* name, int logn, cudaStream_t st);
 void trace_end(int idx, cudaStream_t st);
@@ -119,7 +124,7 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
         unsigned long long fl = epi_frac_limit();
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
                       dim3(kEpiThreads), 0, st, eargs));
     }
     return CY_OK;
@@ -151,7 +156,7 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
         unsigned long long fl = epi_frac_limit();
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
                       dim3(kEpiThreads), 0, st, eargs));
     }
     return CY_OK;
@@ -420,7 +425,7 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
         unsigned long long fl = epi_frac_limit();
         void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+        CY_TRY(launch(epi, "epi_modq", r->logn, dim3(epi_blocks(threads, B.h.l32)),
                       dim3(kEpiThreads), 0, st, eargs));
     }
     // the scale vector is read by the kernels above before the stream moves on
@@ -481,7 +486,7 @@ cy_status cy_icrt(cy_ring* r, const uint32_t* d_res, uint64_t* d_x, int batch, c
         unsigned long long fl = epi_frac_limit();
         void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj, (void*)&fl};
         long long threads = (long long)nj * r->n;
-        CY_TRY(launch(epi, "epi_modq", r->logn, dim3((unsigned)((threads + kEpiThreads - 1) / kEpiThreads)),
+        CY_TRY(launch(epi, "epi_modq", r->logn, dim3(epi_blocks(threads, B.h.l32)),
                       dim3(kEpiThreads), 0, (cudaStream_t)stream, eargs));
     }
     return CY_OK;

@@ -20,6 +20,14 @@ constexpr int PRIME_TWO_ADIC = 16;  // every table prime is 1 mod 2^16
 //   DECRYPT  round(t*(X mod q)/q) mod t               -> [N] uint64
 enum EpiMode { EPI_MODQ = 0, EPI_YASHE = 1, EPI_DECRYPT = 2 };
 
+// Coefficients per thread of the ICRT epilogue kernel for q of l32 words (the
+// constants of a prime are read once for all of them); the launch grid is
+// ceil(coefficients / (threads * this)).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr int epi_coefs_per_thread(int l32) { return l32 <= 6 ? 2 : 1; }
+
 // Constants of one CRT basis for one ring (N, q). Lives in device memory; the
 // kernels read the per-prime fields of their own prime and the epilogue copies
 // what it needs into shared memory.

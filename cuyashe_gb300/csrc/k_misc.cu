@@ -24,6 +24,7 @@ void fill_n12_e4s(KernelSet& ks);
 void fill_n12_e3s(KernelSet& ks);
 void fill_n12_e4m(KernelSet& ks);
 void fill_n13_e4s(KernelSet& ks);
+void fill_n12_e4t(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -60,6 +61,7 @@ static const VariantTable& variants() {
         add(12, fill_n12_e3s);
         add(12, fill_n12_e4m);
         add(13, fill_n13_e4s);
+        add(12, fill_n12_e4t);
     });
     return T;
 }

@@ -449,12 +449,19 @@ __device__ __forceinline__ uint64_t barrett(const Cols<L>& x, const uint32_t* qn
 // padded prime contributes exactly nothing and the prime loop runs whole
 // groups of three without guards.
 constexpr int KPAD = KMAX + 2;
+
+// Scalars of one prime, read with two 16-byte shared loads.
+struct __align__(16) EpiPrime {
+    uint32_t p, ycon, ycon_sh, fhi, flo;
+    uint32_t F0, F1;  // YASHE: R_i / q in units of 2^-64 (lo, hi)
+    uint32_t pad;
+};
 struct EpiShared {
-    uint32_t p[KPAD], ycon[KPAD], ycon_sh[KPAD], flo[KPAD], fhi[KPAD];
-    uint32_t A0[KPAD * L32MAX];
-    uint32_t A1[KPAD * L32MAX];
-    uint32_t F[KPAD * 2], FM[2];  // YASHE: R_i / q and (q - R_M) / q in units of 2^-64
+    EpiPrime pr[KPAD];
+    __align__(16) uint32_t A0[KPAD * L32MAX];
+    __align__(16) uint32_t A1[KPAD * L32MAX];
     uint32_t B0[L32MAX], B1[L32MAX], qn[L32MAX], qhalf_n[L32MAX];
+    uint32_t FM[2];  // YASHE: (q - R_M) / q in units of 2^-64
 };
 
 // Copy the epilogue constants of basis B into shared memory (threads tid, tid +
@@ -463,27 +470,56 @@ template <int L, int MODE>
 __device__ __forceinline__ void epi_stage(EpiShared& S, const BasisDev* __restrict__ B, int tid, int nthreads) {
     const int k = B->k, kp = 3 * ((k + 2) / 3);
     for (int i = tid; i < kp; i += nthreads) {
-        const bool in = i < k;
-        S.p[i] = in ? B->p[i] : 1u;
-        S.ycon[i] = in ? B->ycon[i] : 0u;
-        S.ycon_sh[i] = in ? B->ycon_sh[i] : 0u;
-        S.flo[i] = in ? B->flo[i] : 0u;
-        S.fhi[i] = in ? B->fhi[i] : 0u;
+        EpiPrime e{1u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        if (i < k) {
+            e.p = B->p[i];
+            e.ycon = B->ycon[i];
+            e.ycon_sh = B->ycon_sh[i];
+            e.fhi = B->fhi[i];
+            e.flo = B->flo[i];
+            if (MODE == EPI_YASHE) {
+                e.F0 = B->frac[i][0];
+                e.F1 = B->frac[i][1];
+            }
+        }
+        S.pr[i] = e;
     }
     for (int i = tid; i < kp * L; i += nthreads) {
         const bool in = i < k * L;
         S.A0[i] = in ? B->A0[i / L][i % L] : 0u;
         if (MODE == EPI_YASHE) S.A1[i] = in ? B->A1[i / L][i % L] : 0u;
     }
-    if (MODE == EPI_YASHE) {
-        for (int i = tid; i < kp * 2; i += nthreads) S.F[i] = i < k * 2 ? B->frac[i / 2][i % 2] : 0u;
-        if (tid < 2) S.FM[tid] = B->frac_m[tid];
-    }
+    if (MODE == EPI_YASHE && tid < 2) S.FM[tid] = B->frac_m[tid];
     for (int i = tid; i < L; i += nthreads) {
         S.B0[i] = B->B0[i];
         S.B1[i] = B->B1[i];
         S.qn[i] = B->qn[i];
         S.qhalf_n[i] = B->qhalf_n[i];
+    }
+}
+
+// Row of L words of shared memory (16- or 8-byte loads when L allows).
+template <int L>
+__device__ __forceinline__ void load_row(const uint32_t* src, uint32_t (&a)[L]) {
+    if constexpr (L % 4 == 0) {
+#pragma unroll
+        for (int w = 0; w < L; w += 4) {
+            const uint4 v = *reinterpret_cast<const uint4*>(src + w);
+            a[w] = v.x;
+            a[w + 1] = v.y;
+            a[w + 2] = v.z;
+            a[w + 3] = v.w;
+        }
+    } else if constexpr (L % 2 == 0) {
+#pragma unroll
+        for (int w = 0; w < L; w += 2) {
+            const uint2 v = *reinterpret_cast<const uint2*>(src + w);
+            a[w] = v.x;
+            a[w + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int w = 0; w < L; w++) a[w] = src[w];
     }
 }
 
@@ -497,8 +533,8 @@ __device__ __noinline__ uint64_t yashe_round_exact(const EpiShared& S, const Bas
     Cols<L> c1;
     c1.zero();
     for (int i = 0; i < k; i++) {
-        const uint32_t p = S.p[i];
-        const uint32_t y = red(shoup(__ldcg(r0 + (size_t)i * stride), S.ycon[i], S.ycon_sh[i], p), p);
+        const EpiPrime P = S.pr[i];
+        const uint32_t y = red(shoup(__ldcg(r0 + (size_t)i * stride), P.ycon, P.ycon_sh, P.p), P.p);
         c1.mac(y, &S.A1[i * L]);
         if (i % 3 == 2) c1.norm();
     }
@@ -510,9 +546,10 @@ __device__ __noinline__ uint64_t yashe_round_exact(const EpiShared& S, const Bas
     return barrett<L>(c1, S.qn, B->mu, rdummy);
 }
 
-// Epilogue of one coefficient: r0 points at its residue for prime 0, residues of
-// the next primes follow `stride` words apart. Writes limb j of `dst` (MODQ,
-// YASHE) or one word (DECRYPT).
+// Epilogue of C coefficients: r0[c] points at the residue of coefficient c for
+// prime 0, residues of the next primes follow `stride` words apart. Writes the
+// limbs of dst[c] (MODQ, YASHE) or one word (DECRYPT) where store[c] is set.
+// The constants of a prime are read once for all C coefficients.
 //
 // YASHE rounding: Q = round(S'/q) is first estimated in 64-bit fixed point,
 // Z = sum y_i F_i + v F_M + 2^63 (F = floor(R 2^64 / q)), which undershoots the
@@ -520,111 +557,159 @@ __device__ __noinline__ uint64_t yashe_round_exact(const EpiShared& S, const Bas
 // unless the fraction of Z is within 2^-28 of the next integer; those
 // coefficients (about one in 2^28), and all of them when frac_limit is 0, take
 // the exact multiword path.
-template <int L, int MODE>
-__device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __restrict__ B,
-                                         const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst,
-                                         uint64_t frac_limit = 0) {
+template <int L, int MODE, int C>
+__device__ __forceinline__ void epi_coefs(const EpiShared& S, const BasisDev* __restrict__ B,
+                                          const uint32_t* const (&r0)[C], size_t stride, uint64_t* const (&dst)[C],
+                                          const bool (&store)[C], uint64_t frac_limit) {
     const int k = B->k, shift = B->shift, l64 = B->l64;
     const int groups = (k + 2) / 3;
     const uint64_t mu = B->mu;
-    Cols<L> c0;
-    Cols<2> fz;  // YASHE: Z in 32-bit columns
-    c0.zero();
-    fz.zero();
-    uint64_t vacc = 0;
-    // One prime's contribution: y = [X Mhat_i^-1]_{p_i}, the fixed-point estimate
-    // of y/p_i for v, y times the row of constants into the columns and (YASHE)
-    // y F_i into Z.
-    auto absorb = [&](int i, uint32_t r) {
-        const uint32_t p = S.p[i];
-        const uint32_t y = red(shoup(r, S.ycon[i], S.ycon_sh[i], p), p);
-        vacc += (uint64_t)y * S.fhi[i] + __umulhi(y, S.flo[i]);  // sum y_i/p_i in 2^-32 units
-        c0.mac(y, &S.A0[i * L]);
-        if (MODE == EPI_YASHE) fz.mac(y, &S.F[i * 2]);
+    Cols<L> c0[C];
+    Cols<2> fz[C];  // YASHE: Z in 32-bit columns
+    uint64_t vacc[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        c0[c].zero();
+        fz[c].zero();
+        vacc[c] = 0;
+    }
+    // One prime's contribution to every coefficient: y = [X Mhat_i^-1]_{p_i}, the
+    // fixed-point estimate of y/p_i for v, y times the row of constants into the
+    // columns and (YASHE) y F_i into Z.
+    auto absorb = [&](int i, const uint32_t (&r)[C]) {
+        const EpiPrime P = S.pr[i];
+        uint32_t a[L];
+        load_row<L>(&S.A0[i * L], a);
+        const uint32_t F[2] = {P.F0, P.F1};
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const uint32_t y = red(shoup(r[c], P.ycon, P.ycon_sh, P.p), P.p);
+            vacc[c] += (uint64_t)y * P.fhi + __umulhi(y, P.flo);  // sum y_i/p_i in 2^-32 units
+            c0[c].mac(y, a);
+            if (MODE == EPI_YASHE) fz[c].mac(y, F);
+        }
     };
     // Residues come from L2: the loads of the next two groups of three primes are
     // in flight while a group is absorbed. Loads past the last prime re-read its
     // residue (a valid address); its padded factors make the contribution zero.
-    auto load3 = [&](int g, uint32_t (&d)[3]) {
+    auto load3 = [&](int g, uint32_t (&d)[3][C]) {
 #pragma unroll
-        for (int j = 0; j < 3; j++) d[j] = __ldcg(r0 + (size_t)min(3 * g + j, k - 1) * stride);
+        for (int j = 0; j < 3; j++) {
+            const size_t off = (size_t)min(3 * g + j, k - 1) * stride;
+#pragma unroll
+            for (int c = 0; c < C; c++) d[j][c] = __ldcg(r0[c] + off);
+        }
     };
-    uint32_t g0[3], g1[3], g2[3];
+    uint32_t g0[3][C], g1[3][C], g2[3][C];
     load3(0, g0);
     load3(min(1, groups - 1), g1);
     for (int g = 0; g < groups; g++) {
         load3(min(g + 2, groups - 1), g2);
 #pragma unroll
         for (int j = 0; j < 3; j++) absorb(3 * g + j, g0[j]);
-        c0.norm();  // columns take three products of < 2^62 between carry passes
-        if (MODE == EPI_YASHE) fz.norm();
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-            g0[j] = g1[j];
-            g1[j] = g2[j];
-        }
-    }
-    const uint32_t v = (uint32_t)((vacc + 0x80000000ULL) >> 32);  // round(sum y_i/p_i): X = sum y_i Mhat_i - v M
-    c0.norm();
-    c0.mac(v, S.B0);
-    if (MODE == EPI_YASHE) {
-        fz.mac(v, S.FM);
-        fz.c[1] += 0x80000000u;  // + 1/2
-        fz.norm();
-        const uint64_t frac = fz.c[0] | (fz.c[1] << 32);
-        uint64_t Q2 = fz.c[2] | (fz.c[3] << 32);  // round(S/q) + v, S = sum y_i R_i - v R_M
-        if (frac >= frac_limit) Q2 = yashe_round_exact<L>(S, B, r0, stride, v);
-        // c0 += Q2 << shift
-        const uint64_t lo = Q2 << shift;
-        const uint64_t hi = shift ? (Q2 >> (64 - shift)) : 0;
-        c0.c[0] += (uint32_t)lo;
-        c0.c[1] += (uint32_t)(lo >> 32);
-        c0.c[2] += hi;
-    }
-    c0.norm();
-    uint32_t r[L];
-    barrett<L>(c0, S.qn, mu, r);  // r = (result mod q) << shift
-    if constexpr (MODE == EPI_DECRYPT) {
-        Cols<L> c2;
-        c2.zero();
-        c2.mac(B->t, r);
-        c2.add(S.qhalf_n);
-        c2.norm();
-        uint32_t rd[L];
-        uint64_t Q = barrett<L>(c2, S.qn, mu, rd);  // round(t x / q) in [0, t]
-        if (Q >= B->t) Q -= B->t;
-        dst[0] = Q;
-    } else {
-        uint32_t o[L];
-#pragma unroll
-        for (int w = 0; w < L; w++) {
-            const uint32_t nx = (w + 1 < L) ? r[w + 1] : 0u;
-            o[w] = __funnelshift_r(r[w], nx, shift);
+        for (int c = 0; c < C; c++) {
+            c0[c].norm();  // columns take three products of < 2^62 between carry passes
+            if (MODE == EPI_YASHE) fz[c].norm();
         }
 #pragma unroll
-        for (int j = 0; j < (L + 1) / 2; j++) {
-            const uint64_t lo32 = o[2 * j];
-            const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
-            if (j < l64) dst[j] = lo32 | (hi32 << 32);
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                g0[j][c] = g1[j][c];
+                g1[j][c] = g2[j][c];
+            }
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        const uint32_t v = (uint32_t)((vacc[c] + 0x80000000ULL) >> 32);  // X = sum y_i Mhat_i - v M
+        Cols<L>& x = c0[c];
+        x.norm();
+        x.mac(v, S.B0);
+        if (MODE == EPI_YASHE) {
+            Cols<2>& z = fz[c];
+            z.mac(v, S.FM);
+            z.c[1] += 0x80000000u;  // + 1/2
+            z.norm();
+            const uint64_t frac = z.c[0] | (z.c[1] << 32);
+            uint64_t Q2 = z.c[2] | (z.c[3] << 32);  // round(S/q) + v, S = sum y_i R_i - v R_M
+            if (frac >= frac_limit) Q2 = yashe_round_exact<L>(S, B, r0[c], stride, v);
+            // x += Q2 << shift
+            const uint64_t lo = Q2 << shift;
+            const uint64_t hi = shift ? (Q2 >> (64 - shift)) : 0;
+            x.c[0] += (uint32_t)lo;
+            x.c[1] += (uint32_t)(lo >> 32);
+            x.c[2] += hi;
+        }
+        x.norm();
+        uint32_t r[L];
+        barrett<L>(x, S.qn, mu, r);  // r = (result mod q) << shift
+        if (!store[c]) continue;
+        if constexpr (MODE == EPI_DECRYPT) {
+            Cols<L> c2;
+            c2.zero();
+            c2.mac(B->t, r);
+            c2.add(S.qhalf_n);
+            c2.norm();
+            uint32_t rd[L];
+            uint64_t Q = barrett<L>(c2, S.qn, mu, rd);  // round(t x / q) in [0, t]
+            if (Q >= B->t) Q -= B->t;
+            dst[c][0] = Q;
+        } else {
+            uint32_t o[L];
+#pragma unroll
+            for (int w = 0; w < L; w++) {
+                const uint32_t nx = (w + 1 < L) ? r[w + 1] : 0u;
+                o[w] = __funnelshift_r(r[w], nx, shift);
+            }
+#pragma unroll
+            for (int j = 0; j < (L + 1) / 2; j++) {
+                const uint64_t lo32 = o[2 * j];
+                const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
+                if (j < l64) dst[c][j] = lo32 | (hi32 << 32);
+            }
         }
     }
+}
+
+// One coefficient (the mixed-batch kernel's epilogue units).
+template <int L, int MODE>
+__device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __restrict__ B,
+                                         const uint32_t* __restrict__ r0, size_t stride, uint64_t* __restrict__ dst,
+                                         uint64_t frac_limit = 0) {
+    const uint32_t* const rr[1] = {r0};
+    uint64_t* const dd[1] = {dst};
+    const bool st[1] = {true};
+    epi_coefs<L, MODE, 1>(S, B, rr, stride, dd, st, frac_limit);
 }
 
 template <int L, int MODE>
 __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
                                              void* __restrict__ out, int njobs, unsigned long long frac_limit) {
+    constexpr int C = epi_coefs_per_thread(L);  // coefficients per thread
     __shared__ EpiShared S;
     epi_stage<L, MODE>(S, B, threadIdx.x, blockDim.x);
     __syncthreads();
     const int logn = B->logn, k = B->k, l64 = B->l64;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = 1 << logn;
-    const long long job = idx >> logn;
-    if (job >= njobs) return;
-    const int coef = (int)(idx & (n - 1));
-    uint64_t* dst = reinterpret_cast<uint64_t*>(out) +
-                    (MODE == EPI_DECRYPT ? (size_t)job * n + coef : ((size_t)job * n + coef) * l64);
-    epi_coef<L, MODE>(S, B, resid + (size_t)job * k * n + coef, (size_t)n, dst, frac_limit);
+    const long long total = (long long)njobs << logn;
+    const long long base = (long long)blockIdx.x * blockDim.x * C + threadIdx.x;
+    if (base >= total) return;
+    const uint32_t* r0[C];
+    uint64_t* dst[C];
+    bool store[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        long long idx = base + (long long)c * blockDim.x;  // coalesced across the warp for every c
+        store[c] = idx < total;
+        if (!store[c]) idx = base;  // computed and not written
+        const long long job = idx >> logn;
+        const int coef = (int)(idx & (n - 1));
+        r0[c] = resid + (size_t)job * k * n + coef;
+        dst[c] = reinterpret_cast<uint64_t*>(out) +
+                 (MODE == EPI_DECRYPT ? (size_t)job * n + coef : ((size_t)job * n + coef) * l64);
+    }
+    epi_coefs<L, MODE, C>(S, B, r0, (size_t)n, dst, store, frac_limit);
 }
 
 }  // namespace cy

@@ -101,6 +101,7 @@ extern "C" cy_status cy_polymul_noalloc(cy_ring* r, const uint64_t* d_a, const u
     unsigned long long fl = 0;  // mod-q epilogue: no rounding estimate
     void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch, (void*)&fl};
     const long long threads = (long long)batch * n;
-    return launch_noalloc(epi, "epi_modq_noalloc", B.h.logn, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st,
-                          eargs);
+    const long long per = 256ll * epi_coefs_per_thread(B.h.l32);
+    return launch_noalloc(epi, "epi_modq_noalloc", B.h.logn, dim3((unsigned)((threads + per - 1) / per)), dim3(256),
+                          0, st, eargs);
 }
