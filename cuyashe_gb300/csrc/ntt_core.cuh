@@ -39,7 +39,7 @@ struct NttPlan {
     static constexpr int G = N >> LOGE;  // threads per transform
     static constexpr int NPASS = (LOGN + LOGE - 1) / LOGE;
     static constexpr int R0 = LOGN - (NPASS - 1) * LOGE;  // the first pass takes the remainder
-    static constexpr int SMW = N + (N >> 5);               // padded words per operand buffer
+    static constexpr int SMW = N + (N >> LOGE);            // words per operand buffer (with padding)
     __host__ __device__ static constexpr int R(int pass) { return pass == 0 ? R0 : LOGE; }
     __host__ __device__ static constexpr int S0(int pass) { return pass == 0 ? 0 : R0 + (pass - 1) * LOGE; }
     __host__ __device__ static constexpr int LOGD(int pass) { return LOGN - S0(pass) - R(pass); }
@@ -58,9 +58,30 @@ struct GroupSync {
     }
 };
 
-// one padding word per 32: position -> shared-memory word
-__device__ __forceinline__ int padi(int pos) { return pos + (pos >> 5); }
-__host__ __device__ constexpr int padc(int c) { return c + (c >> 5); }
+// Shared-memory layout of the exchange between two passes whose butterflies
+// span 2^DA and 2^DB positions (LOGD of the writing and the reading pass), for
+// E = 2^R coefficients per thread. For one register slot a warp touches 32
+// consecutive positions when LOGD >= 5, else 32/2^D runs of 2^D positions that
+// are 2^(D+R) apart. Banks are kept distinct on both sides by
+//   * P padding words after every 32 (an address stays base + constant): P = 1
+//     when the strided side has LOGD = 0, P = 2^(5-R) when it has LOGD = R;
+//   * an XOR of the low 5 bits with bits of the row (pos >> 5) when both sides
+//     are strided (LOGD = R and 0), which permutes words inside each 32-word row.
+// Every layout is a bijection into SMW = N + N/2^R words.
+template <int R, int DA, int DB>
+struct XLayout {
+    static constexpr int DMIN = DA < DB ? DA : DB;
+    static constexpr int DMAX = DA < DB ? DB : DA;
+    static constexpr bool SWZ = DMAX < 5 && (R == 3 || R == 4);
+    static constexpr int PAD = (DMIN >= 5 || DMIN == 0 || DMIN != R || R >= 5) ? 1 : (1 << (5 - R));
+    // the padded word of a position whose bits below 5 and above are independent
+    __host__ __device__ static constexpr int pad(int pos) { return pos + PAD * (pos >> 5); }
+    __device__ __forceinline__ static int swz(int pos) {
+        const int x = pos >> 5;
+        if constexpr (R == 3) return pos ^ (x & 7) ^ (((x >> 1) & 3) << 3);
+        else return pos ^ (x & 15) ^ (((x >> 3) & 1) << 4);
+    }
+};
 
 // position of the first element of group v of thread tau in pass PASS
 template <class PL, int PASS>
@@ -145,24 +166,29 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* s
                                          Sync bar = Sync()) {
     constexpr int RA = PL::R(PA), LA = PL::LOGD(PA), NVA = PL::E >> RA;
     constexpr int RB = PL::R(PB), LB = PL::LOGD(PB), NVB = PL::E >> RB;
+    using X = XLayout<PL::LOGE, LA, LB>;
     if (sync_before) bar.sync();
 #pragma unroll
     for (int v = 0; v < NVA; v++) {
-        const int base = padi(group_base<PL, PA>(tau, v));
+        const int g = group_base<PL, PA>(tau, v);  // bits of u << LA are zero in g
+        const int base = X::pad(g);
 #pragma unroll
         for (int u = 0; u < (1 << RA); u++) {
+            const int a = X::SWZ ? X::swz(g | (u << LA)) : base + X::pad(u << LA);
 #pragma unroll
-            for (int o = 0; o < NOPS; o++) sm[o * PL::SMW + base + padc(u << LA)] = x[o][(v << RA) + u];
+            for (int o = 0; o < NOPS; o++) sm[o * PL::SMW + a] = x[o][(v << RA) + u];
         }
     }
     bar.sync();
 #pragma unroll
     for (int v = 0; v < NVB; v++) {
-        const int base = padi(group_base<PL, PB>(tau, v));
+        const int g = group_base<PL, PB>(tau, v);
+        const int base = X::pad(g);
 #pragma unroll
         for (int u = 0; u < (1 << RB); u++) {
+            const int a = X::SWZ ? X::swz(g | (u << LB)) : base + X::pad(u << LB);
 #pragma unroll
-            for (int o = 0; o < NOPS; o++) x[o][(v << RB) + u] = sm[o * PL::SMW + base + padc(u << LB)];
+            for (int o = 0; o < NOPS; o++) x[o][(v << RB) + u] = sm[o * PL::SMW + a];
         }
     }
 }
