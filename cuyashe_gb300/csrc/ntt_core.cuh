@@ -100,6 +100,15 @@ __device__ __forceinline__ int slot_pos(int tau, int e) {
     return group_base<PL, PASS>(tau, e >> R) + ((e & ((1 << R) - 1)) << LOGD);
 }
 
+// Twiddle h of a stage with 2^l twiddles per group. For l >= 1 the group
+// starts at an even index of a 16-byte aligned table, so twiddles h and h+1 come
+// from one 16-byte load (issued at even h; the compiler keeps the odd half).
+__device__ __forceinline__ uint2 load_twiddle(const uint2* __restrict__ twl, int h, int l) {
+    if (l == 0) return __ldg(twl);
+    const uint4 W2 = __ldg(reinterpret_cast<const uint4*>(twl + (h & ~1)));
+    return (h & 1) ? make_uint2(W2.z, W2.w) : make_uint2(W2.x, W2.y);
+}
+
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
                                          int tau) {
@@ -113,10 +122,10 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = 0; l < R; l++) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);
+            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
 #pragma unroll
             for (int h = 0; h < (1 << l); h++) {
-                const uint2 W = __ldg(twl + h);
+                const uint2 W = load_twiddle(twl, h, l);
 #pragma unroll
                 for (int j = 0; j < half; j++) {
                     const int u = (h << (R - l)) + j;
@@ -141,10 +150,10 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = R - 1; l >= 0; l--) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);
+            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
 #pragma unroll
             for (int h = 0; h < (1 << l); h++) {
-                const uint2 W = __ldg(twl + h);
+                const uint2 W = load_twiddle(twl, h, l);
 #pragma unroll
                 for (int j = 0; j < half; j++) {
                     const int u = (h << (R - l)) + j;
