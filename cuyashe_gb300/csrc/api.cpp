@@ -99,6 +99,77 @@ cy_status run_mixed(const std::vector<const cy_polymul_job*>& jobs, cudaStream_t
 cy_status mixed_status(cudaStream_t st);
 bool mixed_supported(const cy_ring* r);
 
+// Two lanes for a call of several chunks: lane 0 is the caller's stream with
+// the workspace's scratch, lane 1 the workspace's side stream with the second
+// scratch. Chunks alternate between them (one chunk's kernels fill the tails
+// of the other's); begin() orders the side stream after the caller's work,
+// end() orders the caller's stream after the side stream's.
+struct Lanes {
+    cudaStream_t s[2] = {nullptr, nullptr};
+    uint32_t* resid[2] = {nullptr, nullptr};
+    bool two = false;
+    cy_status begin(Workspace& ws, cudaStream_t st, size_t words, int nchunks) {
+        CY_TRY(ws.reserve(words));
+        s[0] = s[1] = st;
+        resid[0] = resid[1] = ws.d_resid;
+        two = nchunks > 1;
+        if (!two) return CY_OK;
+        CY_TRY(ws.reserve_side(words));
+        CY_CUDA(cudaEventRecord(ws.fork, st));
+        CY_CUDA(cudaStreamWaitEvent(ws.side, ws.fork, 0));
+        s[1] = ws.side;
+        resid[1] = ws.d_resid2;
+        return CY_OK;
+    }
+    cy_status end(Workspace& ws, cudaStream_t st, cy_status status) {
+        if (!two) return status;
+        const cudaError_t e1 = cudaEventRecord(ws.join, ws.side);
+        const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st, ws.join, 0) : e1;
+        if (status != CY_OK) return status;
+        if (e2 != cudaSuccess) return cuda_error(e2, "joining the side stream");
+        return CY_OK;
+    }
+};
+
+// One chunk of products with basis B: out_j = epilogue(a_j * b_j), residues in `resid`.
+static cy_status product_chunk(const Basis& B, const KernelSet& ks, bool centered, const uint64_t* aj,
+                               long long a_stride, const uint64_t* bj, long long b_stride, void* oj, int nj,
+                               uint32_t* resid, cudaStream_t st) {
+    const int n = B.h.n, k = B.h.k;
+    const BasisDev* Bd = B.d;
+    void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
+    CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
+                  dim3(ks.threads), ks.smem_mul, st, args));
+    unsigned long long fl = epi_frac_limit();
+    void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
+    const long long threads = (long long)nj * n;
+    return launch(epi_kernel(B.h.l32, B.h.mode), epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
+                  dim3(kEpiThreads), 0, st, eargs);
+}
+
+// One chunk of keyswitches c_j -> out_j (out may alias c), residues in `resid`.
+static cy_status keyswitch_chunk(const Basis& B, const KernelSet& ks, int sel, const uint64_t* cj, const uint2* evk,
+                                 int ell, uint64_t* oj, int nj, uint32_t* resid, cudaStream_t st) {
+    const int n = B.h.n, k = B.h.k;
+    const BasisDev* Bd = B.d;
+    void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
+    CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel], st,
+                  args));
+    unsigned long long fl = epi_frac_limit();
+    void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
+    const long long threads = (long long)nj * n;
+    return launch(epi_kernel(B.h.l32, B.h.mode), epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
+                  dim3(kEpiThreads), 0, st, eargs);
+}
+
+static cy_status keyswitch_digits_per_pass(const KernelSet& ks, int ell, int* sel) {
+    int maxsm = 0, dev = 0;
+    CY_CUDA(cudaGetDevice(&dev));
+    CY_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    *sel = (ell % 4 == 0 && ks.smem_ks[1] <= (size_t)maxsm) ? 1 : 0;
+    return CY_OK;
+}
+
 // products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j); `variant`
 // selects the NTT schedule (-1: the tuned one for this device and size)
 static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, long long a_stride,
@@ -109,25 +180,17 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
         B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, centered ? TUNE_MULC : TUNE_MUL));
     const int n = B.h.n, k = B.h.k;
     const int chunk = std::min(batch, chunk_jobs(n, k));
-    CY_TRY(ws.reserve((size_t)chunk * k * n));
-    void* epi = epi_kernel(B.h.l32, B.h.mode);
-    for (int j0 = 0; j0 < batch; j0 += chunk) {
-        int nj = std::min(chunk, batch - j0);
-        const uint64_t* aj = a + (size_t)j0 * a_stride;
-        const uint64_t* bj = b + (size_t)j0 * b_stride;
-        const BasisDev* Bd = B.d;
-        uint32_t* resid = ws.d_resid;
-        void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
-        CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
-                      dim3(ks.threads), ks.smem_mul, st, args));
-        void* oj = (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t);
-        unsigned long long fl = epi_frac_limit();
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
-        long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
-                      dim3(kEpiThreads), 0, st, eargs));
+    const int nchunks = (batch + chunk - 1) / chunk;
+    Lanes L;
+    CY_TRY(L.begin(ws, st, (size_t)chunk * k * n, nchunks));
+    cy_status status = CY_OK;
+    for (int c = 0; c < nchunks && status == CY_OK; c++) {
+        const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
+        status = product_chunk(B, ks, centered, a + (size_t)j0 * a_stride, a_stride, b + (size_t)j0 * b_stride,
+                               b_stride, (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t), nj, L.resid[c & 1],
+                               L.s[c & 1]);
     }
-    return CY_OK;
+    return L.end(ws, st, status);
 }
 
 // keyswitch of `batch` polynomials c_j -> out_j (may alias c)
@@ -138,28 +201,47 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
         kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_KS));
     const int n = B.h.n, k = B.h.k, l64 = B.h.l64;
     const int chunk = std::min(batch, chunk_jobs(n, k));
-    CY_TRY(ws.reserve((size_t)chunk * k * n));
-    int maxsm = 0, dev = 0;
-    CY_CUDA(cudaGetDevice(&dev));
-    CY_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const int sel = (ell % 4 == 0 && ks.smem_ks[1] <= (size_t)maxsm) ? 1 : 0;
-    void* epi = epi_kernel(B.h.l32, B.h.mode);
-    for (int j0 = 0; j0 < batch; j0 += chunk) {
-        int nj = std::min(chunk, batch - j0);
-        const uint64_t* cj = c + (size_t)j0 * n * l64;
-        const BasisDev* Bd = B.d;
-        uint32_t* resid = ws.d_resid;
-        void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
-        CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel],
-                      st, args));
-        uint64_t* oj = out + (size_t)j0 * n * l64;
-        unsigned long long fl = epi_frac_limit();
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
-        long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
-                      dim3(kEpiThreads), 0, st, eargs));
+    const int nchunks = (batch + chunk - 1) / chunk;
+    int sel = 0;
+    CY_TRY(keyswitch_digits_per_pass(ks, ell, &sel));
+    Lanes L;
+    CY_TRY(L.begin(ws, st, (size_t)chunk * k * n, nchunks));
+    cy_status status = CY_OK;
+    for (int cc = 0; cc < nchunks && status == CY_OK; cc++) {
+        const int j0 = cc * chunk, nj = std::min(chunk, batch - j0);
+        status = keyswitch_chunk(B, ks, sel, c + (size_t)j0 * n * l64, evk, ell, out + (size_t)j0 * n * l64, nj,
+                                 L.resid[cc & 1], L.s[cc & 1]);
     }
-    return CY_OK;
+    return L.end(ws, st, status);
+}
+
+// The HE multiply of `batch` pairs: per chunk, the tensor product with the
+// YASHE rounding into out, then (relin) its keyswitch in place; chunks alternate
+// between two lanes.
+cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* evk, int ell, const uint64_t* c1,
+                        const uint64_t* c2, uint64_t* out, int batch, bool do_relin, Workspace& ws, cudaStream_t st) {
+    if (batch == 0) return CY_OK;
+    const int n = tensor.h.n, l64 = tensor.h.l64;
+    const KernelSet& kt = kernel_variant(tensor.h.logn, tuned_variant(tensor.h.logn, l64, TUNE_MULC));
+    const KernelSet& kr = kernel_variant(relin.h.logn, tuned_variant(relin.h.logn, l64, TUNE_KS));
+    const int kmax = std::max(tensor.h.k, do_relin ? relin.h.k : 0);
+    const int chunk = std::min(batch, chunk_jobs(n, kmax));
+    const int nchunks = (batch + chunk - 1) / chunk;
+    int sel = 0;
+    if (do_relin) CY_TRY(keyswitch_digits_per_pass(kr, ell, &sel));
+    const long long stride = (long long)n * l64;
+    Lanes L;
+    CY_TRY(L.begin(ws, st, (size_t)chunk * kmax * n, nchunks));
+    cy_status status = CY_OK;
+    for (int c = 0; c < nchunks && status == CY_OK; c++) {
+        const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
+        uint64_t* oj = out + (size_t)j0 * stride;
+        status = product_chunk(tensor, kt, true, c1 + (size_t)j0 * stride, stride, c2 + (size_t)j0 * stride, stride,
+                               oj, nj, L.resid[c & 1], L.s[c & 1]);
+        if (status == CY_OK && do_relin)
+            status = keyswitch_chunk(relin, kr, sel, oj, evk, ell, oj, nj, L.resid[c & 1], L.s[c & 1]);
+    }
+    return L.end(ws, st, status);
 }
 
 static cy_status run_crt(const Basis& B, const uint64_t* x, uint32_t* res, const uint32_t* d_scale, int batch,

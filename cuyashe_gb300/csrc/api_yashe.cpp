@@ -21,6 +21,8 @@ cy_status check_aligned_api(const void* a, const void* b, const void* c);
 cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long long a_stride, const uint64_t* b,
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
                           cudaStream_t st, int variant = -1);
+cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* evk, int ell, const uint64_t* c1,
+                        const uint64_t* c2, uint64_t* out, int batch, bool do_relin, Workspace& ws, cudaStream_t st);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
                             Workspace& ws, cudaStream_t st, int variant = -1);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
@@ -182,14 +184,11 @@ cy_status cy_yashe_mul_ws(cy_yashe* y, cy_workspace* ws, const uint64_t* d_c1, c
     CY_TRY(check_aligned_api(d_out, nullptr, nullptr));
     if (relin && !y->has_keys) return set_error(CY_ERR_NO_KEYS, "relinearisation needs keys");
     cy_ring* r = y->ring;
-    const long long stride = (long long)r->n * r->l64;
     cudaStream_t st = (cudaStream_t)stream;
     std::unique_lock<std::mutex> lock(r->mu, std::defer_lock);
     Workspace* w = ws ? &ws->ws : &r->own_ws.ws;
     if (!ws) lock.lock();
-    CY_TRY(run_product_api(y->tensor, true, d_c1, stride, d_c2, stride, d_out, stride, batch, *w, st));
-    if (relin) CY_TRY(run_keyswitch_api(y->relin, d_out, y->d_evk, y->ell, d_out, batch, *w, st));
-    return CY_OK;
+    return run_yashe_mul(y->tensor, y->relin, y->d_evk, y->ell, d_c1, d_c2, d_out, batch, relin != 0, *w, st);
 }
 
 cy_status cy_yashe_mul(cy_yashe* y, const uint64_t* d_c1, const uint64_t* d_c2, uint64_t* d_out, int batch,

@@ -67,11 +67,20 @@ cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, c
                       bool mont, bool scale_n, bool centered);
 
 // ---- scratch ------------------------------------------------------------------
+// Residue scratch of the product kernels. Calls of several chunks alternate
+// them between the caller's stream and `side` (created on first use), each
+// with its own scratch, so that one chunk's kernels fill the other's tails;
+// `fork` / `join` order the side stream after and before the caller's.
 struct Workspace {
     int device = -1;
     uint32_t* d_resid = nullptr;
     size_t resid_words = 0;
+    uint32_t* d_resid2 = nullptr;
+    size_t resid2_words = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cy_status reserve(size_t words);
+    cy_status reserve_side(size_t words);  // second scratch, side stream and events
     ~Workspace();
 };
 

@@ -274,8 +274,29 @@ cy_status Workspace::reserve(size_t words) {
     return CY_OK;
 }
 
+cy_status Workspace::reserve_side(size_t words) {
+    if (!side) {
+        CY_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        CY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        CY_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    }
+    if (words <= resid2_words) return CY_OK;
+    if (d_resid2) {
+        cudaFree(d_resid2);
+        d_resid2 = nullptr;
+        resid2_words = 0;
+    }
+    CY_CUDA(cudaMalloc(&d_resid2, words * sizeof(uint32_t)));
+    resid2_words = words;
+    return CY_OK;
+}
+
 Workspace::~Workspace() {
     if (d_resid) cudaFree(d_resid);
+    if (d_resid2) cudaFree(d_resid2);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
 }
 
 }  // namespace cy
