@@ -104,6 +104,8 @@ bool mixed_supported(const cy_ring* r);
 // scratch. Chunks alternate between them (one chunk's kernels fill the tails
 // of the other's); begin() orders the side stream after the caller's work,
 // end() orders the caller's stream after the side stream's.
+static std::atomic<int> g_two_lanes{1};
+
 struct Lanes {
     cudaStream_t s[2] = {nullptr, nullptr};
     uint32_t* resid[2] = {nullptr, nullptr};
@@ -112,7 +114,7 @@ struct Lanes {
         CY_TRY(ws.reserve(words));
         s[0] = s[1] = st;
         resid[0] = resid[1] = ws.d_resid;
-        two = nchunks > 1;
+        two = nchunks > 1 && g_two_lanes.load();
         if (!two) return CY_OK;
         CY_TRY(ws.reserve_side(words));
         CY_CUDA(cudaEventRecord(ws.fork, st));
@@ -511,6 +513,11 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
                       dim3(kEpiThreads), 0, st, eargs));
     }
     // the scale vector is read by the kernels above before the stream moves on
+    return CY_OK;
+}
+
+cy_status cy_set_chunk_overlap(int on) {
+    g_two_lanes.store(on ? 1 : 0);
     return CY_OK;
 }
 

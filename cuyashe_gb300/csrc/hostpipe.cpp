@@ -4,10 +4,12 @@
 // after it, synchronously (Polynomial::update_device_data / update_host_data,
 // src/polynomial.cpp:265-417; cudaDeviceSynchronize, src/common.h:223). Here a
 // host-buffer call is cut into chunks that flow through three slots of device
-// buffers on three streams: while chunk c runs its kernels, chunk c+1 is copied
-// in and chunk c-1 is copied out. With page-locked host buffers the copies run
-// on the copy engines alongside the kernels; pageable buffers give the same
-// result, with copies that do not overlap.
+// buffers: while chunk c runs its kernels, chunk c+1 is copied in and chunk c-1
+// is copied out, on a copy-in stream, two kernel streams (chunks alternate
+// between them so that neighbouring chunks' kernels overlap) and a copy-out
+// stream. With page-locked host buffers the copies run on the copy engines
+// alongside the kernels; pageable buffers give the same result, with copies
+// that do not overlap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,14 +27,14 @@ constexpr int kPipeSlots = 3;
 // the pipeline in turn (the host blocks until a call's last copy is done).
 struct HostPipe {
     std::mutex mu;
-    cudaStream_t s_in = nullptr, s_run = nullptr, s_out = nullptr;
+    cudaStream_t s_in = nullptr, s_run[2] = {nullptr, nullptr}, s_out = nullptr;
     struct Slot {
         uint64_t* d = nullptr;  // in0 | in1 | out, `words` each
         size_t words = 0;
         cudaEvent_t in_done = nullptr, run_done = nullptr, out_done = nullptr;
         bool used = false;
     } slot[kPipeSlots];
-    cy_workspace ws;
+    cy_workspace ws[2];  // one per kernel stream
 };
 
 static HostPipe& host_pipe(int dev) {
@@ -46,9 +48,10 @@ static HostPipe& host_pipe(int dev) {
 
 static cy_status pipe_init(HostPipe& P, int dev) {
     if (P.s_in) return CY_OK;
-    P.ws.ws.device = dev;
+    P.ws[0].ws.device = P.ws[1].ws.device = dev;
     CY_CUDA(cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking));
-    CY_CUDA(cudaStreamCreateWithFlags(&P.s_run, cudaStreamNonBlocking));
+    CY_CUDA(cudaStreamCreateWithFlags(&P.s_run[0], cudaStreamNonBlocking));
+    CY_CUDA(cudaStreamCreateWithFlags(&P.s_run[1], cudaStreamNonBlocking));
     CY_CUDA(cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking));
     for (auto& s : P.slot) {
         CY_CUDA(cudaEventCreateWithFlags(&s.in_done, cudaEventDisableTiming));
@@ -100,12 +103,13 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
             e = cudaMemcpyAsync(in1, h_in1 + off, bytes, cudaMemcpyHostToDevice, P.s_in);
         if (e == cudaSuccess) e = cudaEventRecord(S.in_done, P.s_in);
         // run once the inputs are in and the slot's previous output is out
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_run, S.in_done, 0);
-        if (e == cudaSuccess && S.used) e = cudaStreamWaitEvent(P.s_run, S.out_done, 0);
+        cudaStream_t run = P.s_run[c & 1];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(run, S.in_done, 0);
+        if (e == cudaSuccess && S.used) e = cudaStreamWaitEvent(run, S.out_done, 0);
         if (e != cudaSuccess) break;
-        st = op(&P.ws, in0, h_in1 ? in1 : nullptr, out, nj, P.s_run);
+        st = op(&P.ws[c & 1], in0, h_in1 ? in1 : nullptr, out, nj, run);
         if (st != CY_OK) break;
-        e = cudaEventRecord(S.run_done, P.s_run);
+        e = cudaEventRecord(S.run_done, run);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_out, S.run_done, 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(h_out + off, out, bytes, cudaMemcpyDeviceToHost, P.s_out);
         if (e == cudaSuccess) e = cudaEventRecord(S.out_done, P.s_out);
@@ -113,7 +117,9 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
     }
     // drain every stream, whatever happened above
     const cudaError_t e1 = cudaStreamSynchronize(P.s_in);
-    const cudaError_t e2 = cudaStreamSynchronize(P.s_run);
+    cudaError_t e2 = cudaStreamSynchronize(P.s_run[0]);
+    const cudaError_t e2b = cudaStreamSynchronize(P.s_run[1]);
+    if (e2 == cudaSuccess) e2 = e2b;
     const cudaError_t e3 = cudaStreamSynchronize(P.s_out);
     if (st != CY_OK) return st;
     if (e != cudaSuccess) return cuda_error(e, "host pipeline");

@@ -253,6 +253,14 @@ cy_status cy_yashe_decrypt(cy_yashe *y, const uint64_t *d_ct, uint64_t *d_m, int
  * to calls made after it, process-wide. No counterpart in the reference. */
 cy_status cy_set_epilogue_exact(int on);
 
+/* Calls of several chunks run their chunks on two streams (the caller's and a
+ * side stream of the workspace, with a second residue scratch) so that their
+ * kernels overlap; on == 0 runs them one after another on the caller's stream
+ * (less device memory; clean per-kernel timings). Results are identical.
+ * Process-wide, for calls made after it; default on. No counterpart in the
+ * reference. */
+cy_status cy_set_chunk_overlap(int on);
+
 /* Homomorphic multiply: out = [round(t/q * c1*c2)]_q with the product over
  * Z[x]/(x^N+1) on symmetric representatives, then (relin != 0) the keyswitch
  * [sum_d D_d(out)*evk_d]_q. Replaces Ciphertext::operator* and

@@ -126,3 +126,29 @@ def test_host_entry_points_reject_bad_arguments(cy):
     assert lib.cy_yashe_mul_host(Y.h, buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 1) == NO_KEYS
     assert lib.cy_yashe_mul_host(Y.h, buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 0, 0) == 0
     assert lib.cy_yashe_mul_host(None, buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 0) != 0
+
+
+def test_chunk_overlap_gives_identical_results(cy):
+    """Several chunks run on two streams by default; serial chunks must give the
+    same products and HE multiplies bit for bit."""
+    import torch
+
+    n, t, batch = 4096, 1024, 700  # 227 tensor products per chunk: four chunks
+    Y = cy.Yashe(n, QY, t)
+    Y.keygen(3)
+    rng = np.random.default_rng(9)
+    m = torch.from_numpy(rng.integers(0, t, size=(batch, n), dtype=np.uint64).view(np.int64)).cuda()
+    c1, c2 = Y.encrypt(m, seed=1), Y.encrypt(m.flip(0).contiguous(), seed=2)
+    R = cy.Ring(n, Q127)
+    a = torch.from_numpy(_rand_words(rng, (batch, n, 2), 62).view(np.int64)).cuda()
+    b = torch.from_numpy(_rand_words(rng, (batch, n, 2), 62).view(np.int64)).cuda()
+    lib = cy.lib()
+    outs = []
+    for overlap in (1, 0):
+        lib.cy_set_chunk_overlap(overlap)
+        try:
+            outs.append((Y.mul(c1, c2, relin=True), R.polymul(a, b)))
+            torch.cuda.synchronize()
+        finally:
+            lib.cy_set_chunk_overlap(1)
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
