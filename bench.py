@@ -160,7 +160,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "HE mults/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * pairs / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 (reference CPU multiply, C restatement)",
+        "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 ell=4",
+                   "implementation": "the reference's CPU multiply restated in C (oracle/refpath.c)",
                    "pairs_per_step": pairs, "host_threads": threads},
         "cpu_baseline": {"value": v, "unit": "HE mults/s", "cores": threads, "kind": "port",
                          "sample": "%d HE multiplies per step at N=4096 (29-bit CRT bucket, Goldilocks Stockham NTT)"
