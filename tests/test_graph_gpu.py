@@ -42,3 +42,23 @@ def test_polymul_and_yashe_graphs():
         torch.cuda.synchronize()
         assert torch.equal(o, Y.mul(C1, C2, relin=True))
         C2.copy_(_rand(Y.ring, 64, seed))
+
+
+def test_multi_chunk_yashe_graph_matches_direct_calls():
+    """500 pairs are three chunks, captured on two streams (fork/join events)."""
+    import torch
+
+    import cuyashe_gb300 as cy
+
+    Y = cy.Yashe(4096, Q127, 1024)
+    Y.keygen(12)
+    C1, C2 = _rand(Y.ring, 500, 9), _rand(Y.ring, 500, 10)
+    o = Y.ring.empty(500)
+    g = Y.mul_graph(C1, C2, o, relin=True)
+    s = torch.cuda.Stream()
+    for seed in (13, 14):
+        s.wait_stream(torch.cuda.current_stream())  # inputs written on the current stream
+        g.launch(s)
+        s.synchronize()
+        assert torch.equal(o, Y.mul(C1, C2, relin=True))
+        C1.copy_(_rand(Y.ring, 500, seed))
