@@ -350,7 +350,8 @@ def deep_bench(cy, steps: int, stream):
     return {"workload": "yashe_mul_relin N=16384 log2q=%d t=%d w=2^32 ell=%d" % (q.bit_length(), DEEP_T, info.ell),
             "pairs": DEEP_PAIRS, "he_mults_per_s": DEEP_PAIRS * steps / (total / 1000.0),
             "ms_per_step": total / steps, "tensor_primes": info.tensor_primes, "relin_primes": info.relin_primes,
-            "l2": "256 MB written between timed steps", "kernels": kernels, "decrypt_check": ok}
+            "l2": "256 MB written between timed steps", "kernels": kernels, "decrypt_check": ok,
+            "schedules": ";".join(x for x in cy.tuning_export().split(";") if x.startswith("n16384"))}
 
 
 def time_steps(fn, steps: int, stream):
