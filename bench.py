@@ -556,6 +556,30 @@ def run_ours(args):
         torch.cuda.synchronize()
     poly_plain = plain_calls / (time.perf_counter() - t0)
 
+    # ---- standalone NTT kernel (cy_ntt) against the HBM roofline -----------------
+    # One read and one write of every 32-bit residue per transform are the
+    # algorithmic bytes; [4096][9][4096] residues (604 MB, above L2).
+    ntt_line = None
+    try:
+        kq = R.k
+        RES = torch.zeros((PB, kq, N), dtype=torch.int32, device="cuda")
+        R.ntt(RES)
+        R.ntt(RES, inverse=True)
+        reps = max(3, args.steps // 4)
+        f_ms = time_steps(lambda: R.ntt(RES), reps, stream)
+        i_ms = time_steps(lambda: R.ntt(RES, inverse=True), reps, stream)
+        nbytes = 2 * RES.numel() * 4
+        fg = nbytes * reps / (f_ms / 1000.0) / 1e9
+        ig = nbytes * reps / (i_ms / 1000.0) / 1e9
+        ntt_line = {"transforms": PB * kq, "n": N, "forward_gbs": round(fg, 1), "inverse_gbs": round(ig, 1),
+                    "peak_gbs": peak, "forward_frac": round(fg / peak, 4), "inverse_frac": round(ig / peak, 4),
+                    "transforms_per_s": PB * kq * reps / (f_ms / 1000.0),
+                    "schedule": ";".join(x for x in cy.tuning_export().split(";") if ".ntt=" in x)}
+        log("standalone NTT:", ntt_line)
+        del RES
+    except Exception as e:
+        log("ntt bench failed:", e)
+
     # ---- mixed batch: 512 products, N over {1024..8192}, q of 62/127/190 bits ---
     mixed = None
     try:
@@ -684,6 +708,7 @@ def run_ours(args):
                     "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
         "mixed_batch": mixed,
         "gpu_encrypt_decrypt": crypt,
+        "ntt_standalone": ntt_line,
         "deep_level": deep,
         "cuda_graph": graphs,
         "serving": serving,

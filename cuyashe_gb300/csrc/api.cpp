@@ -255,20 +255,25 @@ static cy_status run_crt(const Basis& B, const uint64_t* x, uint32_t* res, const
     return launch(crt_kernel(), "crt", B.h.logn, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, st, args);
 }
 
-static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st) {
+static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st,
+                         int variant = -1) {
     if (batch == 0) return CY_OK;
-    const KernelSet& ks = kernel_set(B.h.logn);
+    const KernelSet& ks =
+        kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_NTT));
     const BasisDev* Bd = B.d;
     const uint32_t* ninv = B.d_ninv;
-    void* args[] = {(void*)&Bd, (void*)&res, (void*)&ninv};
-    for (int j0 = 0; j0 < batch; j0 += 65535) {
-        int nj = std::min(65535, batch - j0);
+    for (int j0 = 0; j0 < batch; j0 += 2 * 65535) {  // two jobs per block
+        int nj = std::min(2 * 65535, batch - j0);
         uint32_t* rj = res + (size_t)j0 * B.h.k * B.h.n;
-        args[1] = (void*)&rj;
-        CY_TRY(launch(ks.ntt[inverse ? 1 : 0], inverse ? "ntt_inv" : "ntt_fwd", B.h.logn, dim3(B.h.k, nj),
+        void* args[] = {(void*)&Bd, (void*)&rj, (void*)&ninv, (void*)&nj};
+        CY_TRY(launch(ks.ntt[inverse ? 1 : 0], inverse ? "ntt_inv" : "ntt_fwd", B.h.logn, dim3(B.h.k, (nj + 1) / 2),
                       dim3(ks.threads), ks.smem_ntt, st, args));
     }
     return CY_OK;
+}
+
+cy_status run_ntt_api(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st, int variant) {
+    return run_ntt(B, res, batch, inverse, st, variant);
 }
 
 static cy_status run_addsub(const cy_ring* r, const uint64_t* a, const uint64_t* b, uint64_t* c, int batch, bool sub,

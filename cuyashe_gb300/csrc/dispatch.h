@@ -28,7 +28,7 @@ int variant_count(int logn);
 const KernelSet& kernel_variant(int logn, int v);
 
 // Tuned operations (keys of the autotuner's table).
-enum TuneOp { TUNE_MUL = 0, TUNE_MULC = 1, TUNE_KS = 2, TUNE_OPS = 3 };
+enum TuneOp { TUNE_MUL = 0, TUNE_MULC = 1, TUNE_KS = 2, TUNE_NTT = 3, TUNE_OPS = 4 };
 
 // ICRT epilogue for `l32` words of q and epilogue mode (EpiMode).
 void* epi_kernel(int l32, int mode);

@@ -325,36 +325,76 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
 
 // --------------------------------------------------------------------------
 // k_ntt: in-place transform of residue vectors [batch][k][N], values in [0, p).
-// Forward output in bit-reversed order; inverse includes N^-1.
+// Forward output in bit-reversed order; inverse includes N^-1. A block runs the
+// transforms of two jobs for one prime side by side (shared twiddle loads and
+// barriers); with an odd job count the last block repeats its job and stores it
+// once.
 // --------------------------------------------------------------------------
 template <int LOGN, int LOGE, bool INV>
 __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
-    k_ntt(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv) {
+    k_ntt(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv,
+          int njobs) {
     using PL = NttPlan<LOGN, LOGE>;
     constexpr int E = PL::E;
     constexpr int LAST = PL::NPASS - 1;
     extern __shared__ uint32_t smem[];
     const int tau = threadIdx.x;
     const int prime = blockIdx.x;
-    const int job = blockIdx.y;
+    const int job0 = 2 * blockIdx.y;
+    const bool two = job0 + 1 < njobs;
     const int k = B->k;
     const uint32_t p = B->p[prime];
-    uint32_t* v = res + ((size_t)job * k + prime) * PL::N;
-    uint32_t x[1][E];
-    constexpr int STRIDE = region_stride<PL, 1>();
+    uint32_t* v[2] = {res + ((size_t)job0 * k + prime) * PL::N, res + ((size_t)(two ? job0 + 1 : job0) * k + prime) * PL::N};
+    uint32_t x[2][E];
+    constexpr int STRIDE = region_stride<PL, 2>();
+    // after the last pass a thread's E positions are contiguous (16-byte accesses)
+    constexpr bool VEC = PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE && E % 4 == 0;
     if (!INV) {
 #pragma unroll
-        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, 0>(tau, e)];
-        ntt_forward<PL, 1>(x, B->psi[prime], p, tau, smem, STRIDE, 0);
+        for (int o = 0; o < 2; o++)
 #pragma unroll
-        for (int e = 0; e < E; e++) v[slot_pos<PL, LAST>(tau, e)] = red(red(x[0][e], 2 * p), p);
+            for (int e = 0; e < E; e++) x[o][e] = v[o][slot_pos<PL, 0>(tau, e)];
+        ntt_forward<PL, 2>(x, B->psi[prime], p, tau, smem, STRIDE, 0);
+#pragma unroll
+        for (int o = 0; o < 2; o++) {
+            if (o == 1 && !two) break;
+            if constexpr (VEC) {
+                uint4* d4 = reinterpret_cast<uint4*>(v[o] + group_base<PL, LAST>(tau, 0));
+#pragma unroll
+                for (int h = 0; h < E / 4; h++)
+                    d4[h] = make_uint4(red(red(x[o][4 * h], 2 * p), p), red(red(x[o][4 * h + 1], 2 * p), p),
+                                       red(red(x[o][4 * h + 2], 2 * p), p), red(red(x[o][4 * h + 3], 2 * p), p));
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; e++) v[o][slot_pos<PL, LAST>(tau, e)] = red(red(x[o][e], 2 * p), p);
+            }
+        }
     } else {
         const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
 #pragma unroll
-        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
-        ntt_inverse<PL, 1>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0);
+        for (int o = 0; o < 2; o++) {
+            if constexpr (VEC) {
+                const uint4* s4 = reinterpret_cast<const uint4*>(v[o] + group_base<PL, LAST>(tau, 0));
 #pragma unroll
-        for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
+                for (int h = 0; h < E / 4; h++) {
+                    const uint4 q4 = s4[h];
+                    x[o][4 * h] = q4.x;
+                    x[o][4 * h + 1] = q4.y;
+                    x[o][4 * h + 2] = q4.z;
+                    x[o][4 * h + 3] = q4.w;
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; e++) x[o][e] = v[o][slot_pos<PL, LAST>(tau, e)];
+            }
+        }
+        ntt_inverse<PL, 2>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0);
+#pragma unroll
+        for (int o = 0; o < 2; o++) {
+            if (o == 1 && !two) break;
+#pragma unroll
+            for (int e = 0; e < E; e++) v[o][slot_pos<PL, 0>(tau, e)] = red(shoup(x[o][e], w, ws, p), p);
+        }
     }
 }
 
@@ -748,7 +788,7 @@ void fill_kernel_set(KernelSet& ks) {
     ks.smem_mul = SINGLE_MUL ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
     ks.smem_ks[0] = SINGLE_KS ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
     ks.smem_ks[1] = SINGLE_KS ? (size_t)4 * PL::SMW * 4 : region_bytes<PL, 4>();
-    ks.smem_ntt = region_bytes<PL, 1>();
+    ks.smem_ntt = region_bytes<PL, 2>();
 }
 
 }  // namespace cy

@@ -32,7 +32,9 @@ cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk,
                             Workspace& ws, cudaStream_t st, int variant);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 
-static const char* kOpNames[TUNE_OPS] = {"mul", "mulc", "ks"};
+cy_status run_ntt_api(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st, int variant);
+
+static const char* kOpNames[TUNE_OPS] = {"mul", "mulc", "ks", "ntt"};
 
 static std::mutex g_mu;
 static std::map<std::tuple<int, int, int, int>, int> g_choice;  // (device, logn, l64, op) -> variant
@@ -175,6 +177,30 @@ static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, i
                    &chosen);
 }
 
+// The standalone forward transform (cy_ntt) of `batch` residue vectors; each
+// run transforms a fresh copy of the same input so that outputs can be compared.
+static cy_status tune_ntt(const Basis& B, int batch, cudaStream_t st) {
+    const size_t words = (size_t)batch * B.h.k * B.h.n;
+    std::vector<uint32_t> h(words);
+    uint64_t s = 5;
+    for (size_t i = 0; i < words; i++) {
+        s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+        h[i] = (uint32_t)((s >> 33) % B.h.p[(i / B.h.n) % B.h.k]);
+    }
+    DevBuf src;
+    CY_CUDA(cudaMalloc(&src.p, words * sizeof(uint32_t)));
+    CY_CUDA(cudaMemcpy(src.p, h.data(), words * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    int chosen = 0;
+    return tune_op(B.h.logn, B.h.l64, TUNE_NTT, words * sizeof(uint32_t), st,
+                   [&](int v, void* out) {
+                       cudaError_t e = cudaMemcpyAsync(out, src.p, words * sizeof(uint32_t),
+                                                       cudaMemcpyDeviceToDevice, st);
+                       if (e != cudaSuccess) return cuda_error(e, "autotune copy");
+                       return run_ntt_api(B, (uint32_t*)out, batch, false, st, v);
+                   },
+                   &chosen);
+}
+
 }  // namespace cy
 
 using namespace cy;
@@ -184,7 +210,8 @@ extern "C" {
 cy_status cy_ring_autotune(cy_ring* r, int batch, cy_stream_t stream) {
     if (!r || batch < 1) return set_error(CY_ERR_INVALID_ARGUMENT, "bad argument");
     std::lock_guard<std::mutex> lock(r->mu);
-    return tune_product(r->mul, false, batch, (cudaStream_t)stream);
+    CY_TRY(tune_product(r->mul, false, batch, (cudaStream_t)stream));
+    return tune_ntt(r->plain, batch, (cudaStream_t)stream);
 }
 
 cy_status cy_yashe_autotune(cy_yashe* y, int batch, cy_stream_t stream) {

@@ -5,6 +5,8 @@ and each output is compared bit-exactly with the oracle.
 """
 import random
 
+import numpy as np
+
 import pytest
 
 from oracle import ring
@@ -27,7 +29,7 @@ def cy():
     cuyashe_gb300.lib()
     yield cuyashe_gb300
     cuyashe_gb300.tuning_import(";".join("n%d.l%d.%s=0" % (n, l, op) for n in (1024, 2048, 4096, 8192, 16384)
-                                         for l in (1, 2, 3, 6) for op in ("mul", "mulc", "ks")))
+                                         for l in (1, 2, 3, 6) for op in ("mul", "mulc", "ks", "ntt")))
 
 
 def _variants(cy, n, L, op):
@@ -107,3 +109,26 @@ def test_autotune_chooses_and_exports(cy):
     with pytest.raises(cy.CyError):
         cy.tuning_import("garbage")
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("n,q", [(1024, Q62), (4096, Q127), (8192, Q127), (16384, Q62)])
+def test_every_ntt_schedule_agrees(cy, n, q):
+    """cy_ntt under every schedule: the same forward transform as the default,
+    and the inverse gives the input back (5 jobs: two per block plus one alone)."""
+    import torch
+
+    R = cy.Ring(n, q)
+    rng = np.random.default_rng(n)
+    res = np.stack([rng.integers(0, p, size=(5, n), dtype=np.int64) for p in R.primes], axis=1).astype(np.int32)
+    base = torch.from_numpy(res).cuda()
+    vs = _variants(cy, n, R.L, "ntt")
+    outs = []
+    for v in vs:
+        cy.tuning_import("n%d.l%d.ntt=%d" % (n, R.L, v))
+        x = base.clone()
+        R.ntt(x)
+        outs.append(x.clone())
+        R.ntt(x, inverse=True)
+        assert torch.equal(x, base)
+    cy.tuning_import("n%d.l%d.ntt=0" % (n, R.L))
+    assert all(torch.equal(o, outs[0]) for o in outs)
