@@ -207,7 +207,7 @@ def _q380():
     return p
 
 
-def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2024):
+def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2024, batch_budget_us=0):
     import numpy as np
     import torch
 
@@ -231,7 +231,7 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     picks = rng.integers(0, 8, size=(count, 2))
     outs = [np.zeros((256,) + c["ct"].shape[1:], np.uint64) for c in classes]  # reused cyclically
 
-    srv = Server(budget_bytes=120 << 30, streams=4, max_batch=256)
+    srv = Server(budget_bytes=120 << 30, streams=4, max_batch=256, batch_budget_us=batch_budget_us)
     ids = [srv.register(c["y"]) for c in classes]
     # warm-up: one batch per class
     warm = [srv.submit(ids[k], c["ct"][0], c["ct"][1], outs[k][0]) for k, c in enumerate(classes)]
@@ -254,6 +254,7 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     served = {"requests": count, "offered_rate_per_s": rate_per_s, "throughput_per_s": st.throughput_per_s,
               "p50_ms": st.p50_us / 1000.0, "p99_ms": st.p99_us / 1000.0, "mean_ms": st.mean_us / 1000.0,
               "batches": int(st.batches), "failed": int(st.failed), "peak_device_gb": st.peak_device_bytes / 1e9,
+              "batch_budget_us": batch_budget_us,
               "mix": {"%d/%d" % (c["n"], c["qbits"]): c["w"] for c in classes}}
     srv.close()
 
@@ -555,6 +556,17 @@ def run_ours(args):
         R.polymul(A[j:j + 1], Bp[j:j + 1], out=c1p)
         torch.cuda.synchronize()
     poly_plain = plain_calls / (time.perf_counter() - t0)
+    # end to end on page-locked host buffers (copies inside, host wall clock)
+    HA, HB = A.cpu().pin_memory(), Bp.cpu().pin_memory()
+    HC = torch.empty_like(HA).pin_memory()
+    R.polymul_host(HA, HB, out=HC)
+    e2e_reps = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_reps):
+        R.polymul_host(HA, HB, out=HC)
+    poly_e2e = PB * e2e_reps / (time.perf_counter() - t0)
+    poly_e2e_ok = torch.equal(HC, Cp.cpu())
+    del HA, HB, HC
 
     # ---- standalone NTT kernel (cy_ntt) against the HBM roofline -----------------
     # One read and one write of every 32-bit residue per transform are the
@@ -705,7 +717,9 @@ def run_ours(args):
         "kernels": kernels,
         "plain_per_call": {"he_mults_per_s": plain_rate, "batched_over_plain": value / world / plain_rate},
         "polymul": {"batched_per_s": poly_rate, "plain_per_call_per_s": poly_plain,
-                    "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB},
+                    "batched_over_plain": poly_rate / poly_plain, "q_bits": 127, "batch": PB,
+                    "e2e_per_s": poly_e2e, "e2e_matches_device": poly_e2e_ok,
+                    "e2e_api": "cy_polymul_host (page-locked host buffers)"},
         "mixed_batch": mixed,
         "gpu_encrypt_decrypt": crypt,
         "ntt_standalone": ntt_line,

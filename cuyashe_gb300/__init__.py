@@ -65,7 +65,7 @@ class TraceEntry(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device_budget_bytes", ctypes.c_size_t), ("streams", ctypes.c_int), ("max_batch", ctypes.c_int),
-                ("poll_us", ctypes.c_int)]
+                ("poll_us", ctypes.c_int), ("batch_budget_us", ctypes.c_int)]
 
 
 class ServeRequest(ctypes.Structure):

@@ -394,8 +394,10 @@ class Server:
     to them until ``wait`` returns for the ticket.
     """
 
-    def __init__(self, budget_bytes: int, streams: int = 4, max_batch: int = 256, poll_us: int = 20):
-        cfg = ServerConfig(device_budget_bytes=budget_bytes, streams=streams, max_batch=max_batch, poll_us=poll_us)
+    def __init__(self, budget_bytes: int, streams: int = 4, max_batch: int = 256, poll_us: int = 20,
+                 batch_budget_us: int = 0):
+        cfg = ServerConfig(device_budget_bytes=budget_bytes, streams=streams, max_batch=max_batch, poll_us=poll_us,
+                           batch_budget_us=batch_budget_us)
         h = ctypes.c_void_p()
         check(lib().cy_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cy_server_create")
         self.h = h
@@ -406,7 +408,8 @@ class Server:
         if getattr(self, "h", None) and self.h.value:
             lib().cy_server_destroy(self.h)
             self.h = ctypes.c_void_p()
-        self._keep.clear()
+        if getattr(self, "_keep", None):
+            self._keep.clear()
 
     def __del__(self):
         self.close()

@@ -53,6 +53,7 @@ struct Request {
 struct Slot {
     cudaStream_t st = nullptr;
     cudaEvent_t ev = nullptr;
+    cudaEvent_t ev_start = nullptr;  // timing of the batch (time per request of its context)
     cy_workspace ws;
     bool busy = false;
     int cls = -1;
@@ -66,6 +67,7 @@ struct Slot {
         if (h_in) cudaFreeHost(h_in);
         if (h_out) cudaFreeHost(h_out);
         if (ev) cudaEventDestroy(ev);
+        if (ev_start) cudaEventDestroy(ev_start);
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -78,6 +80,7 @@ struct cy_server {
     cy_server_config cfg{};
     int device = 0;
     std::vector<cy_yashe*> classes;
+    std::vector<double> us_per_req;  // per context: running estimate (0: none yet)
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<uint64_t> pending;
@@ -141,6 +144,12 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         const cudaError_t q = cudaEventQuery(s.ev);
         if (q == cudaErrorNotReady) continue;
         Done d{&s, q == cudaSuccess ? CY_OK : cuda_error(q, "serving batch"), {}, 0};
+        float ms = 0;
+        if (q == cudaSuccess && cudaEventElapsedTime(&ms, s.ev_start, s.ev) == cudaSuccess && !s.ids.empty()) {
+            const double per = 1000.0 * ms / (double)s.ids.size();
+            double& est = S->us_per_req[s.cls];
+            est = est > 0 ? 0.8 * est + 0.2 * per : per;
+        }
         const cy_yashe* y = S->classes[s.cls];
         d.poly = (size_t)y->ring->n * y->ring->l64;
         if (s.ids.size() * d.poly > s.cap_words) d.st = set_error(CY_ERR_INTERNAL, "serving slot too small");
@@ -180,10 +189,13 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         const int relin = S->reqs[S->pending.front()].relin;
         cy_yashe* y = S->classes[cls];
         const size_t per = request_bytes(y);
+        int cap = S->cfg.max_batch;  // requests of this batch
+        if (S->cfg.batch_budget_us > 0 && S->us_per_req[cls] > 0)
+            cap = std::max(1, std::min(cap, (int)(S->cfg.batch_budget_us / S->us_per_req[cls])));
         std::vector<uint64_t> take;
         std::vector<const uint64_t*> in1, in2;
         size_t bytes = 0;
-        for (auto it = S->pending.begin(); it != S->pending.end() && (int)take.size() < S->cfg.max_batch;) {
+        for (auto it = S->pending.begin(); it != S->pending.end() && (int)take.size() < cap;) {
             const Request& r = S->reqs[*it];
             if (r.cls != cls || r.relin != relin) {
                 ++it;
@@ -214,8 +226,9 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
                 std::memcpy(s.h_in + i * poly, in1[i], poly * sizeof(uint64_t));
                 std::memcpy(s.h_in + (nb + i) * poly, in2[i], poly * sizeof(uint64_t));
             }
-            cudaError_t e = cudaMemcpyAsync(s.d_in, s.h_in, 2 * nb * poly * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                                            s.st);
+            cudaError_t e = cudaEventRecord(s.ev_start, s.st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(s.d_in, s.h_in, 2 * nb * poly * sizeof(uint64_t), cudaMemcpyHostToDevice, s.st);
             if (e != cudaSuccess) st = cuda_error(e, "serving H2D");
             if (st == CY_OK) st = cy_yashe_mul_ws(y, &s.ws, s.d_in, s.d_in + nb * poly, s.d_out, nb, relin, s.st);
             if (st == CY_OK) {
@@ -275,8 +288,10 @@ extern "C" {
 
 cy_status cy_server_create(const cy_server_config* cfg, cy_server** out) {
     if (!cfg || !out) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (cfg->streams < 1 || cfg->streams > 32 || cfg->max_batch < 1 || cfg->device_budget_bytes == 0)
-        return set_error(CY_ERR_INVALID_ARGUMENT, "streams must be 1..32, max_batch >= 1, budget > 0");
+    if (cfg->streams < 1 || cfg->streams > 32 || cfg->max_batch < 1 || cfg->device_budget_bytes == 0 ||
+        cfg->batch_budget_us < 0)
+        return set_error(CY_ERR_INVALID_ARGUMENT,
+                         "streams must be 1..32, max_batch >= 1, budget > 0, batch_budget_us >= 0");
     std::unique_ptr<cy_server> S(new cy_server());
     S->cfg = *cfg;
     if (S->cfg.poll_us <= 0) S->cfg.poll_us = 20;
@@ -284,7 +299,8 @@ cy_status cy_server_create(const cy_server_config* cfg, cy_server** out) {
     for (int i = 0; i < cfg->streams; i++) {
         std::unique_ptr<Slot> s(new Slot());
         CY_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
-        CY_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+        CY_CUDA(cudaEventCreate(&s->ev));  // timed: batch time per request of its context
+        CY_CUDA(cudaEventCreate(&s->ev_start));
         s->ws.ws.device = S->device;
         S->slots.push_back(std::move(s));
     }
@@ -303,6 +319,7 @@ cy_status cy_server_register(cy_server* S, cy_yashe* y, int* class_id) {
     if (!y->has_keys) return set_error(CY_ERR_NO_KEYS, "context has no keys");
     std::lock_guard<std::mutex> lock(S->mu);
     S->classes.push_back(y);
+    S->us_per_req.push_back(0.0);
     *class_id = (int)S->classes.size() - 1;
     return CY_OK;
 }

@@ -361,6 +361,9 @@ typedef struct cy_server_config {
     int streams;                 /* batches in flight at once (1..32) */
     int max_batch;               /* requests per batch */
     int poll_us;                 /* dispatcher poll period while batches run (default 20) */
+    int batch_budget_us;         /* > 0: a batch of a context takes at most as many requests as fit
+                                    this much GPU time, from a running estimate of the context's
+                                    time per request (0: max_batch only) */
 } cy_server_config;
 typedef struct cy_serve_request {
     int class_id;                /* from cy_server_register */

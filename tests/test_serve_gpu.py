@@ -147,3 +147,37 @@ def test_bad_requests_refused_on_host(setup):
         srv.wait(123456789)
     srv.close()
     tiny.close()
+
+
+def test_time_budget_splits_batches(setup):
+    """With batch_budget_us a context's batches are capped by its measured time
+    per request: a burst is served in more batches, with the same results."""
+    import torch
+
+    cy, Server, ctxs = setup
+    y = ctxs[2]  # N = 4096, 127-bit q
+    rng = np.random.default_rng(11)
+    reqs = [(_uniform(rng, y.n, y.q, y.L), _uniform(rng, y.n, y.q, y.L)) for _ in range(8)]
+    outs = {}
+    for budget in (0, 1):  # 1 us: one request per batch once the estimate exists
+        srv = Server(budget_bytes=2 << 30, streams=1, max_batch=256, batch_budget_us=budget)
+        c = srv.register(y)
+        srv.wait(srv.submit(c, reqs[0][0], reqs[0][1], np.zeros_like(reqs[0][0])))  # first estimate
+        srv.reset_stats()
+        res = [np.zeros_like(a) for a, _ in reqs * 8]
+        tickets = [srv.submit(c, a, b, o) for (a, b), o in zip(reqs * 8, res)]
+        for t in tickets:
+            srv.wait(t)
+        st = srv.stats()
+        assert st.completed == len(tickets) and st.failed == 0
+        outs[budget] = (res, st.batches)
+        srv.close()
+    assert outs[1][1] == len(reqs) * 8  # one request per batch under a 1 us budget
+    for a, b in zip(outs[0][0], outs[1][0]):
+        assert np.array_equal(a, b)
+    alone = y.mul(torch.from_numpy(reqs[0][0].view(np.int64))[None].cuda(),
+                  torch.from_numpy(reqs[0][1].view(np.int64))[None].cuda(), relin=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(alone[0].cpu().numpy().view(np.uint64), outs[1][0][0])
+    with pytest.raises(cy.CyError):
+        Server(budget_bytes=2 << 30, streams=1, max_batch=4, batch_budget_us=-1)
