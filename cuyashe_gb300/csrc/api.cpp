@@ -99,36 +99,54 @@ cy_status run_mixed(const std::vector<const cy_polymul_job*>& jobs, cudaStream_t
 cy_status mixed_status(cudaStream_t st);
 bool mixed_supported(const cy_ring* r);
 
-// Two lanes for a call of several chunks: lane 0 is the caller's stream with
-// the workspace's scratch, lane 1 the workspace's side stream with the second
-// scratch. Chunks alternate between them (one chunk's kernels fill the tails
-// of the other's); begin() orders the side stream after the caller's work,
-// end() orders the caller's stream after the side stream's.
+// Lanes for a call of several chunks: lane 0 is the caller's stream with the
+// workspace's scratch, lanes 1.. side streams of the workspace with their own
+// scratch. Chunk c runs on lane c mod lanes (one chunk's kernels fill the tails
+// of the others'); begin() orders the side streams after the caller's work,
+// end() orders the caller's stream after theirs. The lane count is
+// CY_CHUNK_LANES (1 .. 1 + kMaxSide, default 2); cy_set_chunk_overlap(0) makes it 1.
 static std::atomic<int> g_two_lanes{1};
 
+static int lane_count() {
+    static const int v = [] {
+        const char* e = std::getenv("CY_CHUNK_LANES");
+        const int x = e ? std::atoi(e) : 2;
+        return x < 1 ? 1 : (x > 1 + kMaxSide ? 1 + kMaxSide : x);
+    }();
+    return g_two_lanes.load() ? v : 1;
+}
+
 struct Lanes {
-    cudaStream_t s[2] = {nullptr, nullptr};
-    uint32_t* resid[2] = {nullptr, nullptr};
-    bool two = false;
+    cudaStream_t s[1 + kMaxSide] = {};
+    uint32_t* resid[1 + kMaxSide] = {};
+    int n = 1;
     cy_status begin(Workspace& ws, cudaStream_t st, size_t words, int nchunks) {
         CY_TRY(ws.reserve(words));
-        s[0] = s[1] = st;
-        resid[0] = resid[1] = ws.d_resid;
-        two = nchunks > 1 && g_two_lanes.load();
-        if (!two) return CY_OK;
-        CY_TRY(ws.reserve_side(words));
+        s[0] = st;
+        resid[0] = ws.d_resid;
+        n = std::min(nchunks, lane_count());
+        if (n < 1) n = 1;
+        if (n == 1) return CY_OK;
+        for (int i = 0; i < n - 1; i++) CY_TRY(ws.reserve_side(i, words));
         CY_CUDA(cudaEventRecord(ws.fork, st));
-        CY_CUDA(cudaStreamWaitEvent(ws.side, ws.fork, 0));
-        s[1] = ws.side;
-        resid[1] = ws.d_resid2;
+        for (int i = 0; i < n - 1; i++) {
+            CY_CUDA(cudaStreamWaitEvent(ws.side[i], ws.fork, 0));
+            s[1 + i] = ws.side[i];
+            resid[1 + i] = ws.d_side_resid[i];
+        }
         return CY_OK;
     }
+    cudaStream_t stream(int c) const { return s[c % n]; }
+    uint32_t* scratch(int c) const { return resid[c % n]; }
     cy_status end(Workspace& ws, cudaStream_t st, cy_status status) {
-        if (!two) return status;
-        const cudaError_t e1 = cudaEventRecord(ws.join, ws.side);
-        const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st, ws.join, 0) : e1;
+        cudaError_t err = cudaSuccess;
+        for (int i = 0; i < n - 1; i++) {
+            cudaError_t e = cudaEventRecord(ws.join[i], ws.side[i]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ws.join[i], 0);
+            if (err == cudaSuccess) err = e;
+        }
         if (status != CY_OK) return status;
-        if (e2 != cudaSuccess) return cuda_error(e2, "joining the side stream");
+        if (err != cudaSuccess) return cuda_error(err, "joining the side streams");
         return CY_OK;
     }
 };
@@ -189,8 +207,8 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
     for (int c = 0; c < nchunks && status == CY_OK; c++) {
         const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
         status = product_chunk(B, ks, centered, a + (size_t)j0 * a_stride, a_stride, b + (size_t)j0 * b_stride,
-                               b_stride, (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t), nj, L.resid[c & 1],
-                               L.s[c & 1]);
+                               b_stride, (char*)out + (size_t)j0 * out_stride * sizeof(uint64_t), nj, L.scratch(c),
+                               L.stream(c));
     }
     return L.end(ws, st, status);
 }
@@ -212,7 +230,7 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
     for (int cc = 0; cc < nchunks && status == CY_OK; cc++) {
         const int j0 = cc * chunk, nj = std::min(chunk, batch - j0);
         status = keyswitch_chunk(B, ks, sel, c + (size_t)j0 * n * l64, evk, ell, out + (size_t)j0 * n * l64, nj,
-                                 L.resid[cc & 1], L.s[cc & 1]);
+                                 L.scratch(cc), L.stream(cc));
     }
     return L.end(ws, st, status);
 }
@@ -239,9 +257,9 @@ cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* ev
         const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
         uint64_t* oj = out + (size_t)j0 * stride;
         status = product_chunk(tensor, kt, true, c1 + (size_t)j0 * stride, stride, c2 + (size_t)j0 * stride, stride,
-                               oj, nj, L.resid[c & 1], L.s[c & 1]);
+                               oj, nj, L.scratch(c), L.stream(c));
         if (status == CY_OK && do_relin)
-            status = keyswitch_chunk(relin, kr, sel, oj, evk, ell, oj, nj, L.resid[c & 1], L.s[c & 1]);
+            status = keyswitch_chunk(relin, kr, sel, oj, evk, ell, oj, nj, L.scratch(c), L.stream(c));
     }
     return L.end(ws, st, status);
 }

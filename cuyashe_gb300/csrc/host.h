@@ -67,20 +67,21 @@ cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, c
                       bool mont, bool scale_n, bool centered);
 
 // ---- scratch ------------------------------------------------------------------
-// Residue scratch of the product kernels. Calls of several chunks alternate
-// them between the caller's stream and `side` (created on first use), each
-// with its own scratch, so that one chunk's kernels fill the other's tails;
-// `fork` / `join` order the side stream after and before the caller's.
+// Residue scratch of the product kernels. Calls of several chunks spread them
+// over the caller's stream and up to kMaxSide side streams (created on first
+// use), each with its own scratch, so that one chunk's kernels fill the others'
+// tails; `fork` / `join` order the side streams after and before the caller's.
+constexpr int kMaxSide = 3;
 struct Workspace {
     int device = -1;
     uint32_t* d_resid = nullptr;
     size_t resid_words = 0;
-    uint32_t* d_resid2 = nullptr;
-    size_t resid2_words = 0;
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    uint32_t* d_side_resid[kMaxSide] = {};
+    size_t side_words[kMaxSide] = {};
+    cudaStream_t side[kMaxSide] = {};
+    cudaEvent_t fork = nullptr, join[kMaxSide] = {};
     cy_status reserve(size_t words);
-    cy_status reserve_side(size_t words);  // second scratch, side stream and events
+    cy_status reserve_side(int i, size_t words);  // scratch, stream and events of side lane i
     ~Workspace();
 };
 

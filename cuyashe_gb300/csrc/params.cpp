@@ -274,29 +274,31 @@ cy_status Workspace::reserve(size_t words) {
     return CY_OK;
 }
 
-cy_status Workspace::reserve_side(size_t words) {
-    if (!side) {
-        CY_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-        CY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-        CY_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+cy_status Workspace::reserve_side(int i, size_t words) {
+    if (!fork) CY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (!side[i]) {
+        CY_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+        CY_CUDA(cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming));
     }
-    if (words <= resid2_words) return CY_OK;
-    if (d_resid2) {
-        cudaFree(d_resid2);
-        d_resid2 = nullptr;
-        resid2_words = 0;
+    if (words <= side_words[i]) return CY_OK;
+    if (d_side_resid[i]) {
+        cudaFree(d_side_resid[i]);
+        d_side_resid[i] = nullptr;
+        side_words[i] = 0;
     }
-    CY_CUDA(cudaMalloc(&d_resid2, words * sizeof(uint32_t)));
-    resid2_words = words;
+    CY_CUDA(cudaMalloc(&d_side_resid[i], words * sizeof(uint32_t)));
+    side_words[i] = words;
     return CY_OK;
 }
 
 Workspace::~Workspace() {
     if (d_resid) cudaFree(d_resid);
-    if (d_resid2) cudaFree(d_resid2);
+    for (int i = 0; i < kMaxSide; i++) {
+        if (d_side_resid[i]) cudaFree(d_side_resid[i]);
+        if (join[i]) cudaEventDestroy(join[i]);
+        if (side[i]) cudaStreamDestroy(side[i]);
+    }
     if (fork) cudaEventDestroy(fork);
-    if (join) cudaEventDestroy(join);
-    if (side) cudaStreamDestroy(side);
 }
 
 }  // namespace cy
