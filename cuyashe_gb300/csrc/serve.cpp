@@ -7,7 +7,9 @@
 //     (the oldest request's first, up to max_batch requests, FIFO within them)
 //     when a slot is free and the device-memory budget has room for their
 //     inputs, outputs and residue scratch;
-//   * copies the batch's host ciphertexts into pinned staging, then on the
+//   * copies the batch's host ciphertexts into pinned staging (spread over a
+//     small pool of copy threads, so that host copies do not serialise on the
+//     dispatcher), then on the
 //     slot's stream: one host-to-device copy, cy_yashe_mul_ws on the slot's own
 //     workspace, one device-to-host copy, an event;
 //   * retires batches whose event has completed, copies the results to the
@@ -50,6 +52,73 @@ struct Request {
     size_t bytes = 0;
 };
 
+// Host copies of a batch, spread over a few threads (the caller takes part).
+struct CopyTask {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+
+class CopyPool {
+   public:
+    explicit CopyPool(int threads) {
+        for (int i = 0; i < threads; i++) th_.emplace_back([this] { loop(); });
+    }
+    ~CopyPool() {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+    // Copies every task; returns when all are done.
+    void run(const std::vector<CopyTask>& tasks) {
+        if (tasks.size() < 4 || th_.empty()) {
+            for (const CopyTask& t : tasks) std::memcpy(t.dst, t.src, t.bytes);
+            return;
+        }
+        std::unique_lock<std::mutex> l(mu_);
+        tasks_ = &tasks;
+        next_.store(0);
+        busy_ = (int)th_.size();
+        gen_++;
+        l.unlock();
+        cv_.notify_all();
+        work();
+        l.lock();
+        cv_done_.wait(l, [this] { return busy_ == 0; });
+        tasks_ = nullptr;
+    }
+
+   private:
+    void work() {
+        const std::vector<CopyTask>& t = *tasks_;
+        for (size_t i = next_.fetch_add(1); i < t.size(); i = next_.fetch_add(1)) std::memcpy(t[i].dst, t[i].src, t[i].bytes);
+    }
+    void loop() {
+        uint64_t seen = 0;
+        std::unique_lock<std::mutex> l(mu_);
+        for (;;) {
+            cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+            l.unlock();
+            work();
+            l.lock();
+            if (--busy_ == 0) cv_done_.notify_all();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, cv_done_;
+    const std::vector<CopyTask>* tasks_ = nullptr;
+    std::atomic<size_t> next_{0};
+    int busy_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
 struct Slot {
     cudaStream_t st = nullptr;
     cudaEvent_t ev = nullptr;
@@ -87,6 +156,7 @@ struct cy_server {
     std::unordered_map<uint64_t, Request> reqs;
     uint64_t next_id = 1;
     std::vector<std::unique_ptr<Slot>> slots;
+    std::unique_ptr<CopyPool> copies;
     size_t in_use = 0, peak = 0;
     bool stop = false;
     std::thread worker;
@@ -158,10 +228,12 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
     }
     if (!done.empty()) {
         lock.unlock();
+        std::vector<CopyTask> tasks;
         for (const Done& d : done)
             if (d.st == CY_OK)
                 for (size_t i = 0; i < d.outs.size(); i++)
-                    std::memcpy(d.outs[i], d.s->h_out + i * d.poly, d.poly * sizeof(uint64_t));
+                    tasks.push_back({d.outs[i], d.s->h_out + i * d.poly, d.poly * sizeof(uint64_t)});
+        S->copies->run(tasks);
         lock.lock();
         const double t = now_us();
         for (const Done& d : done) {
@@ -222,10 +294,13 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         cy_status st = grow_slot(s, nb, poly);
         if (st == CY_OK && (size_t)nb * poly > s.cap_words) st = set_error(CY_ERR_INTERNAL, "serving slot too small");
         if (st == CY_OK) {
+            std::vector<CopyTask> tasks;
+            tasks.reserve(2 * nb);
             for (int i = 0; i < nb; i++) {
-                std::memcpy(s.h_in + i * poly, in1[i], poly * sizeof(uint64_t));
-                std::memcpy(s.h_in + (nb + i) * poly, in2[i], poly * sizeof(uint64_t));
+                tasks.push_back({s.h_in + i * poly, in1[i], poly * sizeof(uint64_t)});
+                tasks.push_back({s.h_in + (nb + i) * poly, in2[i], poly * sizeof(uint64_t)});
             }
+            S->copies->run(tasks);
             cudaError_t e = cudaEventRecord(s.ev_start, s.st);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(s.d_in, s.h_in, 2 * nb * poly * sizeof(uint64_t), cudaMemcpyHostToDevice, s.st);
@@ -304,6 +379,7 @@ cy_status cy_server_create(const cy_server_config* cfg, cy_server** out) {
         s->ws.ws.device = S->device;
         S->slots.push_back(std::move(s));
     }
+    S->copies.reset(new CopyPool(3));
     S->worker = std::thread(worker_loop, S.get());
     *out = S.release();
     return CY_OK;
