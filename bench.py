@@ -233,8 +233,10 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
 
     srv = Server(budget_bytes=120 << 30, streams=4, max_batch=256, batch_budget_us=batch_budget_us)
     ids = [srv.register(c["y"]) for c in classes]
-    # warm-up: one batch per class
-    warm = [srv.submit(ids[k], c["ct"][0], c["ct"][1], outs[k][0]) for k, c in enumerate(classes)]
+    # warm-up: a burst of every class, so that slots and workspaces have grown to
+    # the batch sizes of the run before it is timed
+    warm = [srv.submit(ids[k], c["ct"][i % 8], c["ct"][c["pool"] + (i * 3) % 8], outs[k][i])
+            for k, c in enumerate(classes) for i in range(64)]
     for t in warm:
         srv.wait(t)
     srv.reset_stats()

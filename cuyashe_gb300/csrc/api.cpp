@@ -38,13 +38,13 @@ int trace_begin(const char* name, int logn, cudaStream_t st);
 void trace_end(int idx, cudaStream_t st);
 
 // Jobs per launch: the residue scratch of one chunk (k residues of N words per
-// job) is kept near CY_CHUNK_BYTES (default 32 MiB) so that it stays in L2
+// job) is kept near CY_CHUNK_BYTES (default 24 MiB) so that it stays in L2
 // between the NTT kernel that writes it and the epilogue that reads it.
 static long long chunk_bytes() {
     static long long v = [] {
         const char* e = std::getenv("CY_CHUNK_BYTES");
         long long x = e ? std::atoll(e) : 0;
-        return x > 0 ? x : (32ll << 20);
+        return x > 0 ? x : (24ll << 20);
     }();
     return v;
 }

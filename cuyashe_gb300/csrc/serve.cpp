@@ -177,9 +177,12 @@ static size_t request_bytes(const cy_yashe* y) {
 
 // Slots serve every registered context, whose polynomials differ in size:
 // capacity is counted in words, not polynomials.
+// Growing frees and allocates (cudaFree waits for the whole device), so a slot
+// grows to twice what the batch needs: few growths once the load settles.
 static cy_status grow_slot(Slot& s, size_t polys, size_t poly_words) {
-    const size_t words = polys * poly_words;
-    if (words <= s.cap_words) return CY_OK;
+    const size_t need = polys * poly_words;
+    if (need <= s.cap_words) return CY_OK;
+    const size_t words = std::max(2 * need, 2 * s.cap_words);
     if (s.d_in) cudaFree(s.d_in);
     if (s.d_out) cudaFree(s.d_out);
     if (s.h_in) cudaFreeHost(s.h_in);

@@ -45,7 +45,7 @@ def test_polymul_and_yashe_graphs():
 
 
 def test_multi_chunk_yashe_graph_matches_direct_calls():
-    """500 pairs are three chunks, captured on two streams (fork/join events)."""
+    """500 pairs are several chunks, captured on two streams (fork/join events)."""
     import torch
 
     import cuyashe_gb300 as cy
