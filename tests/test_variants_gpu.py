@@ -93,6 +93,39 @@ def test_every_tensor_and_keyswitch_schedule_matches_oracle(cy):
         assert list(out[0]) == exp_r, "keyswitch schedule %d" % v
 
 
+def test_every_keyswitch_schedule_at_16384_matches_oracle(cy):
+    """N = 16384, 380-bit q (12 digits, six-limb kernels): the four-digit pass does
+    not fit in shared memory, so each schedule runs its small-digit kernel (two
+    digits per pass, or one). The keyswitch is a fixed function of c and the
+    evaluation keys, so random keys stand in for generated ones."""
+    import torch
+
+    from oracle.yashe import YasheKeys
+
+    n, t = 16384, 1024
+    q = ring.largest_prime_below(2**380, 2**16)
+    oy = OYashe(YasheParams(n=n, q=q, t=t, w_bits=32))
+    rng = random.Random(16)
+    ell = oy.p.ell
+    evk = [[rng.randrange(q) for _ in range(n)] for _ in range(ell)]
+    keys = YasheKeys(f=[1] + [0] * (n - 1), h=[0] * n, evk=evk)
+    c = [rng.randrange(q) for _ in range(n)]
+    exp = oy.keyswitch(keys, c)
+    Y = cy.Yashe(n, q, t)
+    Y.set_keys(keys.f, keys.h, keys.evk)
+    R = Y.ring
+    assert Y.ell == ell == 12 and R.L == 6
+    C = R.upload([c])
+    vs = _variants(cy, n, R.L, "ks")
+    assert len(vs) >= 2
+    for v in vs:
+        cy.tuning_import("n%d.l%d.ks=%d" % (n, R.L, v))
+        out = R.download(Y.keyswitch(C))
+        torch.cuda.synchronize()
+        assert list(out[0]) == exp, "keyswitch schedule %d" % v
+    cy.tuning_import("n%d.l%d.ks=0" % (n, R.L))
+
+
 def test_autotune_chooses_and_exports(cy):
     import torch
 
