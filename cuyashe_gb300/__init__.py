@@ -162,6 +162,7 @@ SIGNATURES = {
     "cy_tuning_export": ([ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], _i),
     "cy_tuning_import": ([ctypes.c_char_p], _i),
     "cy_set_epilogue_exact": ([_i], _i),
+    "cy_set_epilogue_generic": ([_i], _i),
     "cy_set_chunk_overlap": ([_i], _i),
     "cy_launch_count": ([], ctypes.c_uint64),
     "cy_trace_start": ([], _i),

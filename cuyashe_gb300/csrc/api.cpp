@@ -87,6 +87,25 @@ static const char* epi_name(int mode) {
     return mode == EPI_YASHE ? "epi_yashe" : mode == EPI_DECRYPT ? "epi_decrypt" : "epi_modq";
 }
 
+// Epilogues specialised for the basis's prime count are used unless this is set.
+static std::atomic<int> g_epi_generic{0};
+
+// ICRT epilogue of basis B over `nj` jobs of residues [job][k][N] into `out`: the
+// kernel specialised for B's prime count (constants passed by value) when there
+// is one, else the generic kernel.
+static cy_status launch_epi(const Basis& B, const uint32_t* resid, void* out, int nj, cudaStream_t st,
+                            const char* name) {
+    const BasisDev* Bd = B.d;
+    unsigned long long fl = epi_frac_limit();
+    const dim3 grid(epi_blocks((long long)nj * B.h.n, B.h.l32));
+    if (B.epi && !g_epi_generic.load()) {
+        void* args[] = {(void*)B.epi_param.data(), (void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
+        return launch(B.epi->func, name, B.h.logn, grid, dim3(kEpiThreads), 0, st, args);
+    }
+    void* args[] = {(void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
+    return launch(epi_kernel(B.h.l32, B.h.mode), name, B.h.logn, grid, dim3(kEpiThreads), 0, st, args);
+}
+
 static cy_status check_device(int device) {
     int cur = -1;
     CY_CUDA(cudaGetDevice(&cur));
@@ -155,31 +174,23 @@ struct Lanes {
 static cy_status product_chunk(const Basis& B, const KernelSet& ks, bool centered, const uint64_t* aj,
                                long long a_stride, const uint64_t* bj, long long b_stride, void* oj, int nj,
                                uint32_t* resid, cudaStream_t st) {
-    const int n = B.h.n, k = B.h.k;
+    const int k = B.h.k;
     const BasisDev* Bd = B.d;
     void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
     CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
                   dim3(ks.threads), ks.smem_mul, st, args));
-    unsigned long long fl = epi_frac_limit();
-    void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
-    const long long threads = (long long)nj * n;
-    return launch(epi_kernel(B.h.l32, B.h.mode), epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
-                  dim3(kEpiThreads), 0, st, eargs);
+    return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
 }
 
 // One chunk of keyswitches c_j -> out_j (out may alias c), residues in `resid`.
 static cy_status keyswitch_chunk(const Basis& B, const KernelSet& ks, int sel, const uint64_t* cj, const uint2* evk,
                                  int ell, uint64_t* oj, int nj, uint32_t* resid, cudaStream_t st) {
-    const int n = B.h.n, k = B.h.k;
+    const int k = B.h.k;
     const BasisDev* Bd = B.d;
     void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
     CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel], st,
                   args));
-    unsigned long long fl = epi_frac_limit();
-    void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
-    const long long threads = (long long)nj * n;
-    return launch(epi_kernel(B.h.l32, B.h.mode), epi_name(B.h.mode), B.h.logn, dim3(epi_blocks(threads, B.h.l32)),
-                  dim3(kEpiThreads), 0, st, eargs);
+    return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
 }
 
 static cy_status keyswitch_digits_per_pass(const KernelSet& ks, int ell, int* sel) {
@@ -521,19 +532,11 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
     CY_TRY(ws.reserve((size_t)chunk * k * n + 2 * (size_t)KMAX));
     uint32_t* d_scale = ws.d_resid + (size_t)chunk * k * n;
     CY_CUDA(cudaMemcpyAsync(d_scale, scale.data(), sizeof(uint32_t) * scale.size(), cudaMemcpyHostToDevice, st));
-    void* epi = epi_kernel(B.h.l32, EPI_MODQ);
     for (int j0 = 0; j0 < batch; j0 += chunk) {
         int nj = std::min(chunk, batch - j0);
         const uint64_t* aj = d_a + (size_t)j0 * n * r->l64;
         CY_TRY(run_crt(B, aj, ws.d_resid, d_scale, nj, st));
-        const BasisDev* Bd = B.d;
-        uint32_t* resid = ws.d_resid;
-        uint64_t* oj = d_c + (size_t)j0 * n * r->l64;
-        unsigned long long fl = epi_frac_limit();
-        void* eargs[] = {(void*)&Bd, (void*)&resid, (void*)&oj, (void*)&nj, (void*)&fl};
-        long long threads = (long long)nj * n;
-        CY_TRY(launch(epi, "epi_modq", r->logn, dim3(epi_blocks(threads, B.h.l32)),
-                      dim3(kEpiThreads), 0, st, eargs));
+        CY_TRY(launch_epi(B, ws.d_resid, d_c + (size_t)j0 * n * r->l64, nj, st, "epi_modq"));
     }
     // the scale vector is read by the kernels above before the stream moves on
     return CY_OK;
@@ -541,6 +544,11 @@ cy_status cy_poly_scalar_mul(cy_ring* r, const uint64_t* d_a, const uint64_t* h_
 
 cy_status cy_set_chunk_overlap(int on) {
     g_two_lanes.store(on ? 1 : 0);
+    return CY_OK;
+}
+
+cy_status cy_set_epilogue_generic(int on) {
+    g_epi_generic.store(on ? 1 : 0);
     return CY_OK;
 }
 
@@ -589,17 +597,10 @@ cy_status cy_icrt(cy_ring* r, const uint32_t* d_res, uint64_t* d_x, int batch, c
     CY_TRY(validate_poly_args(r, d_res, d_x, d_x, batch));
     if (batch == 0) return CY_OK;
     const Basis& B = r->plain;
-    const BasisDev* Bd = B.d;
-    void* epi = epi_kernel(B.h.l32, EPI_MODQ);
     for (int j0 = 0; j0 < batch; j0 += 65536) {
         int nj = std::min(65536, batch - j0);
         const uint32_t* rj = d_res + (size_t)j0 * B.h.k * r->n;
-        uint64_t* xj = d_x + (size_t)j0 * r->n * r->l64;
-        unsigned long long fl = epi_frac_limit();
-        void* eargs[] = {(void*)&Bd, (void*)&rj, (void*)&xj, (void*)&nj, (void*)&fl};
-        long long threads = (long long)nj * r->n;
-        CY_TRY(launch(epi, "epi_modq", r->logn, dim3(epi_blocks(threads, B.h.l32)),
-                      dim3(kEpiThreads), 0, (cudaStream_t)stream, eargs));
+        CY_TRY(launch_epi(B, rj, d_x + (size_t)j0 * r->n * r->l64, nj, (cudaStream_t)stream, "epi_modq"));
     }
     return CY_OK;
 }

@@ -33,6 +33,16 @@ enum TuneOp { TUNE_MUL = 0, TUNE_MULC = 1, TUNE_KS = 2, TUNE_NTT = 3, TUNE_OPS =
 // ICRT epilogue for `l32` words of q and epilogue mode (EpiMode).
 void* epi_kernel(int l32, int mode);
 
+// Epilogue specialised for a prime count (k_epi_k): the kernel, the size of its
+// first parameter (the basis constants by value) and the function that writes
+// that parameter from a basis. Null when (l32, k, mode) has no specialisation.
+struct EpiSpecial {
+    void* func;
+    size_t param_bytes;
+    void (*fill)(const BasisDev& h, void* param);
+};
+const EpiSpecial* epi_special(int l32, int k, int mode);
+
 // Bytes of shared memory an exchange region set needs, and whether the kernel
 // alternates two regions (one barrier per exchange) or reuses one (two).
 constexpr size_t kSmemDoubleLimit = 200 * 1024;

@@ -51,6 +51,8 @@ struct Basis {
     BasisDev* d = nullptr;
     uint32_t* d_ninv = nullptr;  // [k][2]: N^-1 mod p_i and its Shoup companion
     int crt_bits = 0;
+    const EpiSpecial* epi = nullptr;     // specialised epilogue of this basis, if any
+    std::vector<unsigned char> epi_param;  // its parameter block (constants by value)
     Basis() = default;
     Basis(const Basis&) = delete;
     Basis& operator=(const Basis&) = delete;

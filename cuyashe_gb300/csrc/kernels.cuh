@@ -752,6 +752,154 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
     epi_coefs<L, MODE, C>(S, B, r0, (size_t)n, dst, store, frac_limit);
 }
 
+// --------------------------------------------------------------------------
+// k_epi_k: the MODQ / YASHE epilogue for a compile-time prime count K. The
+// basis constants travel by value as a kernel parameter (constant bank), so each
+// constant is a uniform operand of the instruction that uses it: no shared-memory
+// staging, no address arithmetic, no guards. The prime loop is straight-line
+// code with a carry pass every four primes (four products of < 2^62 plus a
+// normalised word stay below 2^64).
+// --------------------------------------------------------------------------
+template <int L, int K>
+struct EpiConst {
+    uint32_t p[K], np[K], ycon[K], ycon_sh[K], fhi[K], flo[K], F0[K], F1[K];
+    uint32_t A0[K][L];
+    uint32_t B0[L], qn[L], qhalf_n[L];
+    uint32_t FM[2];
+    uint64_t mu;
+    int shift, l64, logn;
+};
+
+// x in [0, 2m) -> [0, m) with nm = -m
+__device__ __forceinline__ uint32_t red_neg(uint32_t x, uint32_t nm) { return __viaddmin_u32(x, nm, x); }
+
+// The exact YASHE rounding of yashe_round_exact with the constants read from
+// the basis in global memory (the rare path of k_epi_k).
+template <int L>
+__device__ __noinline__ uint64_t yashe_round_exact_g(const BasisDev* __restrict__ B, const uint32_t* __restrict__ r0,
+                                                     size_t stride, uint32_t v) {
+    const int k = B->k;
+    Cols<L> c1;
+    c1.zero();
+    for (int i = 0; i < k; i++) {
+        const uint32_t p = B->p[i];
+        const uint32_t y = red(shoup(__ldcg(r0 + (size_t)i * stride), B->ycon[i], B->ycon_sh[i], p), p);
+        c1.mac(y, B->A1[i]);
+        if (i % 3 == 2) c1.norm();
+    }
+    c1.norm();
+    c1.mac(v, B->B1);
+    c1.add(B->qhalf_n);
+    c1.norm();
+    uint32_t rdummy[L];
+    return barrett<L>(c1, B->qn, B->mu, rdummy);
+}
+
+template <int L, int MODE, int K>
+__global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<L, K> P,
+                                               const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
+                                               void* __restrict__ out, int njobs, unsigned long long frac_limit) {
+    static_assert(MODE == EPI_MODQ || MODE == EPI_YASHE, "mod-q and YASHE epilogues only");
+    constexpr int C = epi_coefs_per_thread(L);
+    const int logn = P.logn;
+    const int n = 1 << logn;
+    const long long total = (long long)njobs << logn;
+    const long long base = (long long)blockIdx.x * blockDim.x * C + threadIdx.x;
+    if (base >= total) return;
+    const uint32_t* r0[C];
+    uint64_t* dst[C];
+    bool store[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        long long idx = base + (long long)c * blockDim.x;  // coalesced across the warp for every c
+        store[c] = idx < total;
+        if (!store[c]) idx = base;  // computed and not written
+        const long long job = idx >> logn;
+        const int coef = (int)(idx & (n - 1));
+        r0[c] = resid + (size_t)job * K * n + coef;
+        dst[c] = reinterpret_cast<uint64_t*>(out) + ((size_t)job * n + coef) * P.l64;
+    }
+    uint32_t r[K][C];
+#pragma unroll
+    for (int i = 0; i < K; i++)
+#pragma unroll
+        for (int c = 0; c < C; c++) r[i][c] = __ldcg(r0[c] + (size_t)i * n);
+
+    Cols<L> c0[C];
+    Cols<2> fz[C];
+    uint64_t vacc[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        c0[c].zero();
+        fz[c].zero();
+        vacc[c] = 0;
+    }
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const uint32_t y = red_neg(shoup(r[i][c], P.ycon[i], P.ycon_sh[i], P.p[i]), P.np[i]);
+            vacc[c] += (uint64_t)y * P.fhi[i] + __umulhi(y, P.flo[i]);  // sum y_i/p_i in 2^-32 units
+#pragma unroll
+            for (int w = 0; w < L; w++) c0[c].c[w] += (uint64_t)y * P.A0[i][w];
+            if (MODE == EPI_YASHE) {
+                fz[c].c[0] += (uint64_t)y * P.F0[i];
+                fz[c].c[1] += (uint64_t)y * P.F1[i];
+            }
+        }
+        if (i % 4 == 3 && i + 1 < K) {
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                c0[c].norm();
+                if (MODE == EPI_YASHE) fz[c].norm();
+            }
+        }
+    }
+    // products since the last carry pass; v adds one more
+    constexpr bool NORM_BEFORE_V = (K % 4 == 0);
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        const uint32_t v = (uint32_t)((vacc[c] + 0x80000000ULL) >> 32);  // X = sum y_i Mhat_i - v M
+        Cols<L>& x = c0[c];
+        if (NORM_BEFORE_V) x.norm();
+#pragma unroll
+        for (int w = 0; w < L; w++) x.c[w] += (uint64_t)v * P.B0[w];
+        if (MODE == EPI_YASHE) {
+            Cols<2>& z = fz[c];
+            if (NORM_BEFORE_V) z.norm();
+            z.c[0] += (uint64_t)v * P.FM[0];
+            z.c[1] += (uint64_t)v * P.FM[1];
+            z.c[1] += 0x80000000u;  // + 1/2
+            z.norm();
+            const uint64_t frac = z.c[0] | (z.c[1] << 32);
+            uint64_t Q2 = z.c[2] | (z.c[3] << 32);  // round(S/q) + v, S = sum y_i R_i - v R_M
+            if (frac >= frac_limit) Q2 = yashe_round_exact_g<L>(B, r0[c], (size_t)n, v);
+            // x += Q2 << shift (each added word < 2^32: the columns stay below 2^64)
+            const uint64_t lo = Q2 << P.shift;
+            const uint64_t hi = P.shift ? (Q2 >> (64 - P.shift)) : 0;
+            x.c[0] += (uint32_t)lo;
+            x.c[1] += (uint32_t)(lo >> 32);
+            x.c[2] += hi;
+        }
+        x.norm();
+        uint32_t rm[L];
+        barrett<L>(x, P.qn, P.mu, rm);  // rm = (result mod q) << shift
+        if (!store[c]) continue;
+        uint32_t o[L];
+#pragma unroll
+        for (int w = 0; w < L; w++) {
+            const uint32_t nx = (w + 1 < L) ? rm[w + 1] : 0u;
+            o[w] = __funnelshift_r(rm[w], nx, P.shift);
+        }
+#pragma unroll
+        for (int j = 0; j < (L + 1) / 2; j++) {
+            const uint64_t lo32 = o[2 * j];
+            const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
+            if (j < P.l64) dst[c][j] = lo32 | (hi32 << 32);
+        }
+    }
+}
+
 }  // namespace cy
 
 namespace cy {

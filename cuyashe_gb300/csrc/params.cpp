@@ -254,6 +254,11 @@ cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, c
         ninv[2 * i] = v;
         ninv[2 * i + 1] = shoup_of(v, p);
     }
+    b.epi = epi_special(b.h.l32, b.h.k, b.h.mode);
+    if (b.epi) {
+        b.epi_param.assign(b.epi->param_bytes, 0);
+        b.epi->fill(b.h, b.epi_param.data());
+    }
     CY_CUDA(cudaMalloc(&b.d, sizeof(BasisDev)));
     CY_CUDA(cudaMemcpy(b.d, &b.h, sizeof(BasisDev), cudaMemcpyHostToDevice));
     CY_CUDA(cudaMalloc(&b.d_ninv, sizeof(uint32_t) * ninv.size()));

@@ -253,6 +253,13 @@ cy_status cy_yashe_decrypt(cy_yashe *y, const uint64_t *d_ct, uint64_t *d_m, int
  * to calls made after it, process-wide. No counterpart in the reference. */
 cy_status cy_set_epilogue_exact(int on);
 
+/* The ICRT epilogue has kernels specialised for the prime counts of common
+ * parameter sets (their basis constants passed by value); on != 0 makes every
+ * call use the generic kernel instead (a cross-check; slower). Results are
+ * identical. Process-wide, for calls made after it; default off. No counterpart
+ * in the reference. */
+cy_status cy_set_epilogue_generic(int on);
+
 /* Calls of several chunks run their chunks on two streams (the caller's and a
  * side stream of the workspace, with a second residue scratch) so that their
  * kernels overlap; on == 0 runs them one after another on the caller's stream

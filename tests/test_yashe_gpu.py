@@ -234,3 +234,52 @@ def test_fixed_point_rounding_at_full_size(cy):
         lib.cy_set_epilogue_exact(0)
     torch.cuda.synchronize()
     assert torch.equal(fast, exact)
+
+
+def _limbs_below(q, shape, rng):
+    """Random coefficients in [0, q) as little-endian limbs, with q-1, (q-1)/2 and
+    (q+1)/2 planted (the centring boundaries)."""
+    L = (q.bit_length() + 63) // 64
+    top = q.bit_length() - 64 * (L - 1) - 1
+    x = rng.integers(0, 2**63, size=shape + (L,), dtype=np.uint64) * np.uint64(2) + np.uint64(1)
+    x[..., L - 1] &= np.uint64((1 << top) - 1)
+    for j, v in enumerate((q - 1, (q - 1) // 2, (q + 1) // 2)):
+        x[0, j] = [(v >> (64 * w)) & (2**64 - 1) for w in range(L)]
+    return x
+
+
+@pytest.mark.parametrize("n,q,t,kt,kr", [(4096, Q127, 1024, 9, 6), (2048, Q62, 65537, 5, 4),
+                                         (8192, Q190, 65537, 14, 8), (16384, Q380, 65537, 26, 15)])
+def test_specialised_epilogues_equal_generic(cy, n, q, t, kt, kr):
+    """The epilogues compiled for these prime counts (constants passed by value)
+    give the generic kernel's results bit for bit: tensor rounding, keyswitch and
+    plain product."""
+    import torch
+
+    Y = cy.Yashe(n, q, t)
+    Y.keygen(3)
+    info = Y.info()
+    assert (info.tensor_primes, info.relin_primes) == (kt, kr)
+    batch = 64 if n <= 4096 else 6
+    rng = np.random.default_rng(n)
+    C1 = torch.from_numpy(_limbs_below(q, (batch, n), rng).view(np.int64)).cuda()
+    C2 = torch.from_numpy(_limbs_below(q, (batch, n), rng).view(np.int64)).cuda()
+    P = cy.Ring(n, q)
+    lib = cy.lib()
+    outs = []
+    for generic in (0, 1):
+        lib.cy_set_epilogue_generic(generic)
+        try:
+            outs.append((Y.mul(C1, C2, relin=False), Y.mul(C1, C2, relin=True), P.polymul(C1, C2)))
+            torch.cuda.synchronize()
+        finally:
+            lib.cy_set_epilogue_generic(0)
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+    # and the oracle's tensor product for the first pair at N <= 4096
+    if n <= 4096:
+        oy = OYashe(YasheParams(n=n, q=q, t=t, w_bits=32))
+        to_int = lambda a: [sum(int(a[i, w]) << (64 * w) for w in range(a.shape[1])) for i in range(n)]
+        h1, h2 = C1[0].cpu().numpy().view(np.uint64), C2[0].cpu().numpy().view(np.uint64)
+        got = outs[0][0][0].cpu().numpy().view(np.uint64)
+        assert to_int(got) == oy.mul_tensor(to_int(h1), to_int(h2))
