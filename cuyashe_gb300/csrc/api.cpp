@@ -97,13 +97,16 @@ static cy_status launch_epi(const Basis& B, const uint32_t* resid, void* out, in
                             const char* name) {
     const BasisDev* Bd = B.d;
     unsigned long long fl = epi_frac_limit();
-    const dim3 grid(epi_blocks((long long)nj * B.h.n, B.h.l32));
+    const long long coefs = (long long)nj * B.h.n;
     if (B.epi && !g_epi_generic.load()) {
+        const long long per = (long long)kEpiThreads * B.epi->coefs_per_thread;
         void* args[] = {(void*)B.epi_param.data(), (void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
-        return launch(B.epi->func, name, B.h.logn, grid, dim3(kEpiThreads), 0, st, args);
+        return launch(B.epi->func, name, B.h.logn, dim3((unsigned)((coefs + per - 1) / per)), dim3(kEpiThreads), 0,
+                      st, args);
     }
     void* args[] = {(void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
-    return launch(epi_kernel(B.h.l32, B.h.mode), name, B.h.logn, grid, dim3(kEpiThreads), 0, st, args);
+    return launch(epi_kernel(B.h.l32, B.h.mode), name, B.h.logn, dim3(epi_blocks(coefs, B.h.l32)), dim3(kEpiThreads),
+                  0, st, args);
 }
 
 static cy_status check_device(int device) {

@@ -40,6 +40,7 @@ struct EpiSpecial {
     void* func;
     size_t param_bytes;
     void (*fill)(const BasisDev& h, void* param);
+    int coefs_per_thread;
 };
 const EpiSpecial* epi_special(int l32, int k, int mode);
 

@@ -82,7 +82,34 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
     std::lock_guard<std::mutex> lock(P.mu);
     CY_TRY(pipe_init(P, dev));
     chunk = std::max(1, std::min(chunk, batch));
-    const int nchunks = (batch + chunk - 1) / chunk;
+    // Chunk sizes: a quarter and a half chunk first, so that the kernels start
+    // after a short copy, and a half and a quarter chunk last, so that the last
+    // kernels and the last copy out are short; whole chunks between.
+    std::vector<int> sizes;
+    {
+        const int q4 = std::max(1, chunk / 4), q2 = std::max(1, chunk / 2);
+        int left = batch;
+        if (left > 2 * chunk + q2 + q4) {
+            sizes.push_back(q4);
+            sizes.push_back(q2);
+            left -= q4 + q2;
+        }
+        while (left > chunk + q2 + q4) {
+            sizes.push_back(chunk);
+            left -= chunk;
+        }
+        if (left > q2 + q4 && batch > 2 * chunk) {
+            sizes.push_back(left - q2 - q4);
+            sizes.push_back(q2);
+            sizes.push_back(q4);
+        } else {
+            while (left > 0) {
+                sizes.push_back(std::min(chunk, left));
+                left -= sizes.back();
+            }
+        }
+    }
+    const int nchunks = (int)sizes.size();
     const int nslots = std::min(kPipeSlots, nchunks);
     const size_t cw = words * (size_t)chunk;
     for (int s = 0; s < nslots; s++) {
@@ -91,8 +118,9 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
     }
     cy_status st = CY_OK;
     cudaError_t e = cudaSuccess;
-    for (int c = 0; c < nchunks && st == CY_OK && e == cudaSuccess; c++) {
-        const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
+    int j0 = 0;
+    for (int c = 0; c < nchunks && st == CY_OK && e == cudaSuccess; j0 += sizes[c], c++) {
+        const int nj = sizes[c];
         HostPipe::Slot& S = P.slot[c % nslots];
         const size_t off = (size_t)j0 * words, bytes = (size_t)nj * words * sizeof(uint64_t);
         uint64_t *in0 = S.d, *in1 = S.d + S.words, *out = S.d + 2 * S.words;

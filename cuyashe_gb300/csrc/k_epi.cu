@@ -45,7 +45,10 @@ struct EpiEntry {
 };
 }  // namespace
 
-#define CY_EPI_K(L, K, MODE) {L, K, MODE, {(void*)k_epi_k<L, MODE, K>, sizeof(EpiConst<L, K>), fill_epi_const<L, K>}}
+// One coefficient per thread: with the constants as instruction operands a
+// second coefficient saves no loads, and half the registers admit more warps.
+#define CY_EPI_K(L, K, MODE) \
+    {L, K, MODE, {(void*)k_epi_k<L, MODE, K, 1>, sizeof(EpiConst<L, K>), fill_epi_const<L, K>, 1}}
 
 static const EpiEntry kEpiSpecial[] = {
     CY_EPI_K(4, 9, EPI_YASHE),   CY_EPI_K(4, 6, EPI_MODQ),  CY_EPI_K(4, 9, EPI_MODQ),

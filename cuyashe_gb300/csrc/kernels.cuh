@@ -795,12 +795,11 @@ __device__ __noinline__ uint64_t yashe_round_exact_g(const BasisDev* __restrict_
     return barrett<L>(c1, B->qn, B->mu, rdummy);
 }
 
-template <int L, int MODE, int K>
+template <int L, int MODE, int K, int C>
 __global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<L, K> P,
                                                const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
                                                void* __restrict__ out, int njobs, unsigned long long frac_limit) {
     static_assert(MODE == EPI_MODQ || MODE == EPI_YASHE, "mod-q and YASHE epilogues only");
-    constexpr int C = epi_coefs_per_thread(L);
     const int logn = P.logn;
     const int n = 1 << logn;
     const long long total = (long long)njobs << logn;
