@@ -26,6 +26,7 @@ void fill_n12_e4m(KernelSet& ks);
 void fill_n13_e4s(KernelSet& ks);
 void fill_n12_e4t(KernelSet& ks);
 void fill_n14_e4d1(KernelSet& ks);
+void fill_n12_e4u(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -64,6 +65,7 @@ static const VariantTable& variants() {
         add(13, fill_n13_e4s);
         add(12, fill_n12_e4t);
         add(14, fill_n14_e4d1);
+        add(12, fill_n12_e4u);
     });
     return T;
 }

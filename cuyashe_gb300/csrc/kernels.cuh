@@ -125,16 +125,28 @@ __device__ __forceinline__ uint32_t crt_words(const uint32_t (&w)[W], const uint
         acc = (j0 == 0) ? f : red(acc + f, 2 * c.p);
     }
     if (CENTER) {
-        // x > (q-1)/2: the top words decide unless they are equal (rare), then
-        // the lower words do
-        bool gt = w[W - 1] > qh[W - 1];
-        if (w[W - 1] == qh[W - 1]) {
-            bool g = false;
+        // x > (q-1)/2: one 64- or 128-bit compare (no branch) for two or four
+        // words; for more, the top words decide unless they are equal (rare),
+        // then the lower words do
+        bool gt;
+        if constexpr (W == 2) {
+            gt = ((uint64_t)w[1] << 32 | w[0]) > ((uint64_t)qh[1] << 32 | qh[0]);
+        } else if constexpr (W == 4) {
+            const unsigned __int128 xv = (unsigned __int128)((uint64_t)w[3] << 32 | w[2]) << 64 |
+                                         ((uint64_t)w[1] << 32 | w[0]);
+            const unsigned __int128 hv = (unsigned __int128)((uint64_t)qh[3] << 32 | qh[2]) << 64 |
+                                         ((uint64_t)qh[1] << 32 | qh[0]);
+            gt = xv > hv;
+        } else {
+            gt = w[W - 1] > qh[W - 1];
+            if (w[W - 1] == qh[W - 1]) {
+                bool g = false;
 #pragma unroll
-            for (int j = 0; j < W - 1; j++) g = (w[j] > qh[j]) || (w[j] == qh[j] && g);
-            gt = g;
+                for (int j = 0; j < W - 1; j++) g = (w[j] > qh[j]) || (w[j] == qh[j] && g);
+                gt = g;
+            }
         }
-        if (gt) acc = acc + 2 * c.p - c.qmodp;  // [0, 4p)
+        acc += gt ? 2 * c.p - c.qmodp : 0u;  // [0, 4p)
     }
     return acc;
 }
