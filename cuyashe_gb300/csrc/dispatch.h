@@ -12,7 +12,7 @@ namespace cy {
 struct KernelSet {
     int logn = 0, loge = 0, threads = 0;
     void* mul[7][2] = {};  // [l64][centered]
-    void* ks[7][2] = {};   // [l64][keyswitch with ND_LO (2 or 1) / 4 digits per pass]
+    void* ks[7][2] = {};   // [l64][keyswitch with ND_LO (2 or 1) / ND_HI (4 or 2) digits per pass]
     void* ntt[2] = {nullptr, nullptr};  // forward / inverse
     size_t smem_mul = 0, smem_ks[2] = {0, 0}, smem_ntt = 0;
     void* mul_for(int l64, bool centered) const { return mul[mul[l64][0] ? l64 : 0][centered ? 1 : 0]; }

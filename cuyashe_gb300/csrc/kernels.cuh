@@ -915,12 +915,12 @@ __global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<
 
 namespace cy {
 
-template <int LOGN, int LOGE, int L64, int MB_MUL, int MB_KS, bool SINGLE_KS, bool SINGLE_MUL, int ND_LO>
+template <int LOGN, int LOGE, int L64, int MB_MUL, int MB_KS, bool SINGLE_KS, bool SINGLE_MUL, int ND_LO, int ND_HI>
 void fill_l64(KernelSet& ks) {
     ks.mul[L64][0] = (void*)k_mul<LOGN, LOGE, L64, false, MB_MUL, SINGLE_MUL>;
     ks.mul[L64][1] = (void*)k_mul<LOGN, LOGE, L64, true, MB_MUL, SINGLE_MUL>;
     ks.ks[L64][0] = (void*)k_keyswitch<LOGN, LOGE, L64, ND_LO, MB_KS, SINGLE_KS>;
-    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, 4, MB_KS, SINGLE_KS>;
+    ks.ks[L64][1] = (void*)k_keyswitch<LOGN, LOGE, L64, ND_HI, MB_KS, SINGLE_KS>;
 }
 
 // SPECIALISE: also instantiate the kernels for 1, 2, 3 and 6 limbs (q of up to
@@ -929,26 +929,27 @@ void fill_l64(KernelSet& ks) {
 // compiled for (0: the defaults above).
 // SINGLE_KS / SINGLE_MUL: the keyswitch / product kernels use one exchange region.
 // ND_LO: digits per pass of the keyswitch kernel used when four do not fit (2, or 1
-// for fewer registers).
+// for fewer registers); ND_HI: digits per pass of the one used when the digit
+// count is a multiple of four and it fits (4, or 2 for fewer registers).
 template <int LOGN, int LOGE, bool SPECIALISE, int MB_MUL = 0, int MB_KS = 0, bool SINGLE_KS = false,
-          bool SINGLE_MUL = false, int ND_LO = 2>
+          bool SINGLE_MUL = false, int ND_LO = 2, int ND_HI = 4>
 void fill_kernel_set(KernelSet& ks) {
     using PL = NttPlan<LOGN, LOGE>;
     ks.logn = LOGN;
     ks.loge = LOGE;
     ks.threads = PL::G;
-    fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO>(ks);
+    fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
     if constexpr (SPECIALISE) {
-        fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO>(ks);
-        fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO>(ks);
-        fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO>(ks);
-        fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO>(ks);
+        fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+        fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+        fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+        fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
     }
     ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
     ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
     ks.smem_mul = SINGLE_MUL ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
     ks.smem_ks[0] = SINGLE_KS ? (size_t)ND_LO * PL::SMW * 4 : region_bytes<PL, ND_LO>();
-    ks.smem_ks[1] = SINGLE_KS ? (size_t)4 * PL::SMW * 4 : region_bytes<PL, 4>();
+    ks.smem_ks[1] = SINGLE_KS ? (size_t)ND_HI * PL::SMW * 4 : region_bytes<PL, ND_HI>();
     ks.smem_ntt = region_bytes<PL, 2>();
 }
 
