@@ -34,7 +34,7 @@ def cy():
 
 def _variants(cy, n, L, op):
     out = []
-    for v in range(8):
+    for v in range(32):
         try:
             cy.tuning_import("n%d.l%d.%s=%d" % (n, L, op, v))
         except cy.CyError:
@@ -51,17 +51,18 @@ def test_every_product_schedule_matches_oracle(cy, n, q):
 
     R = cy.Ring(n, q)
     rng = random.Random(n)
-    a = [[rng.randrange(q) for _ in range(n)] for _ in range(2)]
-    b = [[rng.randrange(q) for _ in range(n)] for _ in range(2)]
+    # three jobs: schedules with two jobs per block also meet an odd tail
+    a = [[rng.randrange(q) for _ in range(n)] for _ in range(3)]
+    b = [[rng.randrange(q) for _ in range(n)] for _ in range(3)]
     A, B = R.upload(a), R.upload(b)
-    exp = [ring.polymul_mod(a[j], b[j], q) for j in range(2)]
+    exp = [ring.polymul_mod(a[j], b[j], q) for j in range(3)]
     vs = _variants(cy, n, R.L, "mul")
     assert vs and vs[0] == 0
     for v in vs:
         cy.tuning_import("n%d.l%d.mul=%d" % (n, R.L, v))
         out = R.download(R.polymul(A, B))
         torch.cuda.synchronize()
-        for j in range(2):
+        for j in range(3):
             assert list(out[j]) == exp[j], "schedule %d" % v
     cy.tuning_import("n%d.l%d.mul=0" % (n, R.L))
 
