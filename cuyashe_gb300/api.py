@@ -232,15 +232,30 @@ class Ring:
         return res
 
 
+class MixedBatch:
+    """A fixed list of products of mixed rings, submitted as one cy_polymul_batched
+    call per run. The job array is built once: for a batch of hundreds of jobs,
+    building it in Python costs about as much as the GPU work."""
+
+    def __init__(self, jobs: Sequence[tuple]):
+        self._jobs = list(jobs)  # keeps the rings and tensors alive
+        self.arr = (PolymulJob * len(self._jobs))()
+        for i, (r, a, b, c) in enumerate(self._jobs):
+            self.arr[i].ring = r.h.value
+            self.arr[i].d_a = _ptr(a)
+            self.arr[i].d_b = _ptr(b)
+            self.arr[i].d_c = _ptr(c)
+
+    def __len__(self) -> int:
+        return len(self._jobs)
+
+    def run(self, stream=None) -> None:
+        check(lib().cy_polymul_batched(self.arr, len(self._jobs), _stream_handle(stream)), "cy_polymul_batched")
+
+
 def polymul_batched(jobs: Sequence[tuple], stream=None) -> None:
     """jobs: (ring, a, b, c) with device tensors; one submission for mixed rings."""
-    arr = (PolymulJob * len(jobs))()
-    for i, (r, a, b, c) in enumerate(jobs):
-        arr[i].ring = r.h.value
-        arr[i].d_a = _ptr(a)
-        arr[i].d_b = _ptr(b)
-        arr[i].d_c = _ptr(c)
-    check(lib().cy_polymul_batched(arr, len(jobs), _stream_handle(stream)), "cy_polymul_batched")
+    MixedBatch(jobs).run(stream)
 
 
 def polymul_batched_status(stream=None) -> None:

@@ -2,9 +2,10 @@
 // (N from 1024 to 8192, q up to 192 bits): the fused CRT -> NTT -> pointwise ->
 // INTT -> ICRT -> mod q path over a work list.
 //
-// Blocks of 512 threads claim units from an atomic counter. The NTT units come
-// first, largest transforms first; a unit of N = 2048 or 1024 runs 2 or 4 primes
-// of its job side by side, each on its own named barrier. The epilogue units of
+// Blocks of 1024 threads claim units from an atomic counter. The NTT units come
+// first, largest transforms first; with 8 coefficients per thread a unit of
+// N = 8192 fills the block and a unit of N = 4096, 2048 or 1024 runs 2, 4 or 8
+// primes of its job side by side, each on its own named barrier. The epilogue units of
 // a job follow all NTT units; a block that claims one waits until every prime of
 // that job is done. Those primes were claimed earlier by running blocks that
 // never wait, so the wait ends; the spin is still bounded, and on expiry the
@@ -13,18 +14,20 @@
 
 namespace cy {
 
-constexpr int kMixedThreads = 512;
+constexpr int kMixedThreads = 1024;
 constexpr unsigned kMixedSpinLimit = 1u << 24;  // ~ seconds with the back-off below
 
-template <int LOGN, int LOGE>
+// L64: limbs per coefficient (1..3, compile-time load and CRT split), or 0 to
+// read the count at run time.
+template <int LOGN, int LOGE, int L64>
 __device__ __forceinline__ void mixed_ntt_unit(const MixedJob& J, const MixedUnit& U, uint32_t* smem,
                                                uint32_t* __restrict__ done) {
     using PL = NttPlan<LOGN, LOGE>;
     constexpr int E = PL::E, G = PL::G;
     constexpr int NSUB = kMixedThreads / G;
-    // exchange regions of one sub-group: double-buffered below 8192, single above
-    constexpr int SUBW = (NSUB > 1 || LOGN < 13) ? 4 * PL::SMW : 2 * PL::SMW;
-    constexpr int STRIDE = (NSUB > 1 || LOGN < 13) ? 2 * PL::SMW : 0;
+    // two exchange regions of two operands per sub-group (147 KB per block at every N)
+    constexpr int SUBW = 4 * PL::SMW;
+    constexpr int STRIDE = 2 * PL::SMW;
     const int sub = threadIdx.x / G, tau = threadIdx.x % G;
     if (sub >= U.count) return;  // fewer primes than sub-groups in this unit
     const int prime = U.first + sub;
@@ -32,13 +35,32 @@ __device__ __forceinline__ void mixed_ntt_unit(const MixedJob& J, const MixedUni
     uint32_t* sm = smem + sub * SUBW;
     const BasisDev* __restrict__ B = J.B;
     const PrimeCtx c = load_prime_ctx(B, prime);
-    const uint32_t* crt = B->crt[prime];
     uint32_t x[2][E];
+    if constexpr (L64 > 0) {
+        constexpr int W = 2 * L64;
+        uint32_t cc[W], qh[W];
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-        const int pos = slot_pos<PL, 0>(tau, e);
-        x[0][e] = crt_coef<false>(J.a, pos, J.l64, crt, nullptr, c);
-        x[1][e] = crt_coef<false>(J.b, pos, J.l64, crt, nullptr, c);
+        for (int w = 0; w < W; w++) {
+            cc[w] = B->crt[prime][w];
+            qh[w] = 0;  // no centring
+        }
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int pos = slot_pos<PL, 0>(tau, e);
+            uint32_t wa[W], wb[W];
+            load_words<L64>(J.a + (size_t)pos * L64, wa);
+            load_words<L64>(J.b + (size_t)pos * L64, wb);
+            x[0][e] = crt_words<W, false>(wa, cc, qh, c);
+            x[1][e] = crt_words<W, false>(wb, cc, qh, c);
+        }
+    } else {
+        const uint32_t* crt = B->crt[prime];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int pos = slot_pos<PL, 0>(tau, e);
+            x[0][e] = crt_coef<false>(J.a, pos, J.l64, crt, nullptr, c);
+            x[1][e] = crt_coef<false>(J.b, pos, J.l64, crt, nullptr, c);
+        }
     }
     int buf = ntt_forward<PL, 2, GroupSync>(x, B->psi[prime], c.p, tau, sm, STRIDE, 0, bar);
     uint32_t z[1][E];
@@ -68,7 +90,7 @@ __device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {
     return v;
 }
 
-__global__ void __launch_bounds__(kMixedThreads, 2)
+__global__ void __launch_bounds__(kMixedThreads, 1)
     k_mixed(const MixedJob* __restrict__ jobs, const MixedUnit* __restrict__ units, int n_units,
             uint32_t* __restrict__ done, uint32_t* __restrict__ ctl) {
     extern __shared__ uint32_t smem[];
@@ -82,11 +104,16 @@ __global__ void __launch_bounds__(kMixedThreads, 2)
         const MixedUnit U = units[u];
         const MixedJob J = jobs[U.job];
         if (U.kind == 0) {
-            switch (J.logn) {
-                case 10: mixed_ntt_unit<10, 3>(J, U, smem, done); break;
-                case 11: mixed_ntt_unit<11, 3>(J, U, smem, done); break;
-                case 12: mixed_ntt_unit<12, 3>(J, U, smem, done); break;
-                case 13: mixed_ntt_unit<13, 4>(J, U, smem, done); break;
+            switch (J.logn * 4 + J.l64) {
+#define CY_MIXED_NTT(LOGN, LOGE)                                                    \
+    case LOGN * 4 + 1: mixed_ntt_unit<LOGN, LOGE, 1>(J, U, smem, done); break; \
+    case LOGN * 4 + 2: mixed_ntt_unit<LOGN, LOGE, 2>(J, U, smem, done); break; \
+    case LOGN * 4 + 3: mixed_ntt_unit<LOGN, LOGE, 3>(J, U, smem, done); break;
+                CY_MIXED_NTT(10, 3)
+                CY_MIXED_NTT(11, 3)
+                CY_MIXED_NTT(12, 3)
+                CY_MIXED_NTT(13, 3)
+#undef CY_MIXED_NTT
                 default: break;
             }
         } else {
@@ -118,7 +145,12 @@ __global__ void __launch_bounds__(kMixedThreads, 2)
 }
 
 void* mixed_kernel() { return (void*)k_mixed; }
-size_t mixed_smem_bytes() { return (size_t)4 * NttPlan<12, 3>::SMW * sizeof(uint32_t); }
+// the same at every N: (1024 / (N/8)) sub-groups x 4 operand buffers of N + N/8 words
+size_t mixed_smem_bytes() { return (size_t)2 * 4 * NttPlan<12, 3>::SMW * sizeof(uint32_t); }
+static_assert(1 * 4 * NttPlan<13, 3>::SMW == 2 * 4 * NttPlan<12, 3>::SMW &&
+                  4 * 4 * NttPlan<11, 3>::SMW == 2 * 4 * NttPlan<12, 3>::SMW &&
+                  8 * 4 * NttPlan<10, 3>::SMW == 2 * 4 * NttPlan<12, 3>::SMW,
+              "one shared-memory size serves every transform length");
 int mixed_threads() { return kMixedThreads; }
 
 }  // namespace cy

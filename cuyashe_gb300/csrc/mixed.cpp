@@ -76,7 +76,8 @@ cy_status run_mixed(const std::vector<const cy_polymul_job*>& jobs, cudaStream_t
         const cy_ring* r = jobs[j]->ring;
         offset[j] = words;
         words += (size_t)r->mul.h.k * r->n;
-        const int per = r->logn == 10 ? 4 : (r->logn == 11 ? 2 : 1);  // primes side by side in one block
+        // primes side by side in one 1024-thread block (8 coefficients per thread)
+        const int per = r->logn == 10 ? 8 : r->logn == 11 ? 4 : r->logn == 12 ? 2 : 1;
         for (int f = 0; f < r->mul.h.k; f += per) ntt_units.push_back({j, 0, f, std::min(per, r->mul.h.k - f)});
     }
     // largest transforms first (longest units first balances the tail)

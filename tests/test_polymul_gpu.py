@@ -310,3 +310,39 @@ def test_mixed_batch_one_launch_config3(cy):
     polymul_batched_status()
     for (R, A, B, C) in jobs[:64]:
         assert torch.equal(R.polymul(A, B), C)
+
+
+def test_prepared_mixed_batch_reruns_on_new_inputs(cy):
+    """A MixedBatch built once gives the per-ring products on every run, also
+    after its input buffers are refilled in place."""
+    import torch
+
+    from cuyashe_gb300.api import MixedBatch, polymul_batched_status
+
+    rng = np.random.default_rng(77)
+    specs = [(1024, Q62), (2048, Q127), (4096, Q190), (8192, Q127), (4096, Q127)] * 8
+    rings = {s: cy.Ring(*s) for s in set(specs)}
+
+    def fill(R, t):
+        L = R.L
+        top = R.q.bit_length() - 64 * (L - 1) - 1
+        x = rng.integers(0, 2**63, size=(1, R.n, L), dtype=np.uint64)
+        x[..., L - 1] &= np.uint64((1 << top) - 1)
+        t.copy_(torch.from_numpy(x.view(np.int64)).cuda())
+
+    jobs = []
+    for s in specs:
+        R = rings[s]
+        A, B, C = R.empty(1), R.empty(1), R.empty(1)
+        fill(R, A)
+        fill(R, B)
+        jobs.append((R, A, B, C))
+    mb = MixedBatch(jobs)
+    assert len(mb) == len(jobs)
+    for _ in range(2):
+        mb.run()
+        polymul_batched_status()
+        for (R, A, B, C) in jobs:
+            assert torch.equal(R.polymul(A, B), C)
+        for (R, A, B, C) in jobs:  # new inputs, same buffers
+            fill(R, A)
