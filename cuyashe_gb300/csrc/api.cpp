@@ -180,8 +180,8 @@ static cy_status product_chunk(const Basis& B, const KernelSet& ks, bool centere
     const int k = B.h.k;
     const BasisDev* Bd = B.d;
     void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
-    CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn, dim3(k, nj),
-                  dim3(ks.threads), ks.smem_mul, st, args));
+    CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn,
+                  dim3(k * ks.blocks_per_prime, nj), dim3(ks.threads), ks.smem_mul, st, args));
     return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
 }
 
@@ -191,8 +191,8 @@ static cy_status keyswitch_chunk(const Basis& B, const KernelSet& ks, int sel, c
     const int k = B.h.k;
     const BasisDev* Bd = B.d;
     void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
-    CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k, nj), dim3(ks.threads), ks.smem_ks[sel], st,
-                  args));
+    CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k * ks.blocks_per_prime, nj),
+                  dim3(ks.threads), ks.smem_ks[sel], st, args));
     return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
 }
 

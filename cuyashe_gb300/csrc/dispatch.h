@@ -15,6 +15,7 @@ struct KernelSet {
     void* ks[7][2] = {};   // [l64][keyswitch with ND_LO (2 or 1) / ND_HI (4 or 2) digits per pass]
     void* ntt[2] = {nullptr, nullptr};  // forward / inverse
     size_t smem_mul = 0, smem_ks[2] = {0, 0}, smem_ntt = 0;
+    int blocks_per_prime = 1;  // product / keyswitch blocks per (prime, job): 2 for block pairs
     void* mul_for(int l64, bool centered) const { return mul[mul[l64][0] ? l64 : 0][centered ? 1 : 0]; }
     void* ks_for(int l64, int nd4) const { return ks[ks[l64][0] ? l64 : 0][nd4]; }
 };

@@ -27,6 +27,7 @@ void fill_n13_e4s(KernelSet& ks);
 void fill_n12_e4t(KernelSet& ks);
 void fill_n14_e4d1(KernelSet& ks);
 void fill_n12_e4u(KernelSet& ks);
+void fill_n14_pair(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -66,6 +67,11 @@ static const VariantTable& variants() {
         add(12, fill_n12_e4t);
         add(14, fill_n14_e4d1);
         add(12, fill_n12_e4u);
+        {
+            KernelSet ks = T.v[14][0];  // the default set's standalone NTT
+            fill_n14_pair(ks);
+            T.v[14].push_back(ks);
+        }
     });
     return T;
 }

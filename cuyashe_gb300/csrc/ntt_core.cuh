@@ -109,9 +109,12 @@ __device__ __forceinline__ uint2 load_twiddle(const uint2* __restrict__ twl, int
     return (h & 1) ? make_uint2(W2.z, W2.w) : make_uint2(W2.x, W2.y);
 }
 
+// tm: twiddle-offset multiplier. A transform of length N is stages 0.. of one of
+// length 2N restricted to half h of it when its stage-s twiddles start at
+// (2 + h) * 2^s instead of 2^s (tm = 2 + h); tm = 1 for a whole transform.
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                         int tau) {
+                                         int tau, int tm = 1) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
     constexpr int NV = PL::E >> R;
@@ -122,7 +125,7 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = 0; l < R; l++) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            const uint2* twl = tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
 #pragma unroll
             for (int h = 0; h < (1 << l); h++) {
                 const uint2 W = load_twiddle(twl, h, l);
@@ -139,7 +142,7 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                         int tau) {
+                                         int tau, int tm = 1) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
     constexpr int NV = PL::E >> R;
@@ -150,7 +153,7 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = R - 1; l >= 0; l--) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (1 << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            const uint2* twl = tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
 #pragma unroll
             for (int h = 0; h < (1 << l); h++) {
                 const uint2 W = load_twiddle(twl, h, l);
@@ -210,13 +213,13 @@ template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct FwdFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
                                               uint32_t p, int tau, uint32_t* sm, int stride, int buf,
-                                              Sync bar = Sync()) {
+                                              Sync bar = Sync(), int tm = 1) {
         if constexpr (PASS >= PL::NPASS) {
             return buf;
         } else {
             exchange<PL, PASS - 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau);
-            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar);
+            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau, tm);
+            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm);
         }
     }
 };
@@ -226,13 +229,13 @@ template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct InvFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
                                               uint32_t p, int tau, uint32_t* sm, int stride, int buf,
-                                              Sync bar = Sync()) {
+                                              Sync bar = Sync(), int tm = 1) {
         if constexpr (PASS < 0) {
             return buf;
         } else {
             exchange<PL, PASS + 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            inv_pass<PL, PASS, NOPS>(x, tw, p, tau);
-            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar);
+            inv_pass<PL, PASS, NOPS>(x, tw, p, tau, tm);
+            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm);
         }
     }
 };
@@ -241,17 +244,19 @@ struct InvFrom {
 // registers in last-pass layout (bit-reversed order).
 template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync()) {
-    fwd_pass<PL, 0, NOPS>(x, tw, p, tau);
-    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar);
+                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
+                                           int tm = 1) {
+    fwd_pass<PL, 0, NOPS>(x, tw, p, tau, tm);
+    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm);
 }
 
 // Full inverse transform: registers in last-pass layout -> pass-0 layout.
 template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync()) {
-    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau);
-    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar);
+                                           int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
+                                           int tm = 1) {
+    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau, tm);
+    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm);
 }
 
 }  // namespace cy

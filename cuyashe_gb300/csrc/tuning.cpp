@@ -103,6 +103,14 @@ static cy_status tune_op(int logn, int l64, int op, size_t out_bytes, cudaStream
     for (int v = 0; v < nv && st_all == CY_OK; v++) {
         void* out = v == 0 ? ref.p : cur.p;
         st_all = run(v, out);  // warm-up and the output to check
+        if (st_all != CY_OK && v > 0) {
+            // a schedule this device cannot launch (e.g. a block-pair cluster that
+            // does not fit) is skipped; launch errors are not sticky
+            cudaGetLastError();
+            if (cudaStreamSynchronize(st) != cudaSuccess) break;
+            st_all = CY_OK;
+            continue;
+        }
         if (st_all != CY_OK) break;
         if (cudaStreamSynchronize(st) != cudaSuccess) {
             st_all = set_error(CY_ERR_CUDA, "autotune warm-up failed");

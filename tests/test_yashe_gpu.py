@@ -165,7 +165,21 @@ def test_deep_level_config(cy):
     got = R.download(out)
     torch.cuda.synchronize()
     assert [int(v) for v in dec[0]] == ring.polymul_mod(m1, m2, t)
-    assert list(got[0]) == oy.mul(keys, c1, c2, relin=True)
+    exp = oy.mul(keys, c1, c2, relin=True)
+    assert list(got[0]) == exp
+    # every N = 16384 schedule of the tensor product and the keyswitch (one-block
+    # and block-pair kernels alike)
+    try:
+        for v in range(32):
+            try:
+                cy.tuning_import("n16384.l6.mulc=%d;n16384.l6.ks=%d" % (v, v))
+            except cy.CyError:
+                break
+            got = R.download(Y.mul(R.upload([c1]), R.upload([c2]), relin=True))
+            torch.cuda.synchronize()
+            assert list(got[0]) == exp, "schedule %d" % v
+    finally:
+        cy.tuning_import("n16384.l6.mulc=0;n16384.l6.ks=0")
 
 
 def test_yashe_add(cy):
