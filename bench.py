@@ -357,6 +357,29 @@ def deep_bench(cy, steps: int, stream):
             "schedules": ";".join(x for x in cy.tuning_export().split(";") if x.startswith("n16384"))}
 
 
+def ncu_deep_step(pairs: int):
+    """One autotuned deep-level HE multiply of `pairs` pairs between
+    cudaProfilerStart/Stop (for ncu --profile-from-start off)."""
+    import numpy as np
+    import torch
+
+    import cuyashe_gb300 as cy
+
+    Y = cy.Yashe(DEEP_N, _q380(), DEEP_T, W_BITS, 8.0)
+    Y.keygen(4242)
+    Y.autotune(batch=pairs)
+    C1, C2, _, _, _, _ = make_inputs(Y, pairs, pool=4, seed=31, n=DEEP_N, t=DEEP_T)
+    out = Y.ring.empty(pairs)
+    for _ in range(3):
+        Y.mul(C1, C2, relin=True, out=out)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    Y.mul(C1, C2, relin=True, out=out)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    log("ncu deep step done:", ";".join(x for x in cy.tuning_export().split(";") if x.startswith("n16384")))
+
+
 def time_steps(fn, steps: int, stream):
     import torch
 
@@ -753,6 +776,8 @@ def main():
                     help="run only the serving measurement over SECONDS of arrivals and print it")
     ap.add_argument("--ncu-step", action="store_true",
                     help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
+    ap.add_argument("--ncu-deep", type=int, default=0, metavar="PAIRS",
+                    help="the same for one autotuned deep-level step (N=16384, 380-bit q) of PAIRS pairs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: warm-up raised to 3")
@@ -764,6 +789,8 @@ def main():
 
         cy.lib()
         print(json.dumps(serving_bench(cy, seconds=args.serving_only)), flush=True)
+    elif args.ncu_deep > 0:
+        ncu_deep_step(args.ncu_deep)
     else:
         run_ours(args)
 
