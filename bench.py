@@ -176,7 +176,10 @@ def run_reference(args):
 # ----------------------------------------------------------------------------
 
 SERVE_CLASSES = [  # (N, q, t, weight): q = largest prime below 2^b with q = 1 (mod 2^16)
-    (2048, 4611686018427322369, 257, 0.4),
+    # t = 17 for the 62-bit q: with t = 257 a relinearised product's noise reaches
+    # half a plaintext step (rounding distance 0.4999) and decryption fails; with
+    # t = 17 the worst distance is 0.009
+    (2048, 4611686018427322369, 17, 0.4),
     (4096, Q_YASHE, 1024, 0.3),
     (8192, 1569275433846670190958947355801916604025588861116000698369, 65537, 0.2),
     (16384, None, 65537, 0.1),
@@ -211,7 +214,7 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     import numpy as np
     import torch
 
-    from cuyashe_gb300.api import Server, Yashe
+    from cuyashe_gb300.api import Ring, Server, Yashe
 
     classes = []
     for n, q, t, w in SERVE_CLASSES:
@@ -222,7 +225,7 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
         rng = np.random.default_rng(n)
         m = rng.integers(0, t, size=(2 * pool, n), dtype=np.uint64)
         ct = y.encrypt_host(m, seed=n)
-        classes.append({"y": y, "w": w, "ct": ct, "pool": pool, "n": n, "qbits": q.bit_length()})
+        classes.append({"y": y, "w": w, "ct": ct, "m": m, "t": t, "pool": pool, "n": n, "qbits": q.bit_length()})
     rng = np.random.default_rng(seed)
     count = int(rate_per_s * seconds)
     arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
@@ -239,6 +242,14 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
             for k, c in enumerate(classes) for i in range(64)]
     for t in warm:
         srv.wait(t)
+    # one served product per class decrypts to m1 * m2 mod t (slot 0 holds
+    # ct[0] * ct[pool]; checked before the timed run reuses the slots)
+    decrypt_ok = True
+    for k, c in enumerate(classes):
+        got = c["y"].decrypt(torch.from_numpy(outs[k][0:1].view(np.int64)).cuda()).cpu().numpy().view(np.uint64)
+        PT = Ring(c["n"], c["t"])
+        exp = PT.polymul(PT.upload([c["m"][0].tolist()]), PT.upload([c["m"][c["pool"]].tolist()]))
+        decrypt_ok = decrypt_ok and bool((got[0] == exp.cpu().numpy().view(np.uint64)[0, :, 0]).all())
     srv.reset_stats()
     tickets = []
     t0 = time.perf_counter()
@@ -256,8 +267,8 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     served = {"requests": count, "offered_rate_per_s": rate_per_s, "throughput_per_s": st.throughput_per_s,
               "p50_ms": st.p50_us / 1000.0, "p99_ms": st.p99_us / 1000.0, "mean_ms": st.mean_us / 1000.0,
               "batches": int(st.batches), "failed": int(st.failed), "peak_device_gb": st.peak_device_bytes / 1e9,
-              "batch_budget_us": batch_budget_us,
-              "mix": {"%d/%d" % (c["n"], c["qbits"]): c["w"] for c in classes}}
+              "batch_budget_us": batch_budget_us, "decrypt_ok": decrypt_ok,
+              "mix": {"%d/%d/t=%d" % (c["n"], c["qbits"], c["t"]): c["w"] for c in classes}}
     srv.close()
 
     # the plain per-request path on the same trace prefix: one multiply per
