@@ -26,6 +26,7 @@ const char* last_error_message();
 void* addsub_kernel(int l64, bool sub);
 void* crt_kernel();
 void* shoup_pairs_kernel();
+void* evk_rows_kernel();
 
 static constexpr int kEpiThreads = 256;
 // blocks of the epilogue kernel for `coefs` coefficients of a q of l32 words
@@ -294,6 +295,11 @@ static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse,
         kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_NTT));
     const BasisDev* Bd = B.d;
     const uint32_t* ninv = B.d_ninv;
+    if (ks.ntt_jobs_per_block == 1) {  // k_ntt1: grid (jobs, primes)
+        void* args[] = {(void*)&Bd, (void*)&res, (void*)&ninv, (void*)&batch};
+        return launch(ks.ntt[inverse ? 1 : 0], inverse ? "ntt_inv" : "ntt_fwd", B.h.logn, dim3(batch, B.h.k),
+                      dim3(ks.threads), ks.smem_ntt, st, args);
+    }
     for (int j0 = 0; j0 < batch; j0 += 2 * 65535) {  // two jobs per block
         int nj = std::min(2 * 65535, batch - j0);
         uint32_t* rj = res + (size_t)j0 * B.h.k * B.h.n;
@@ -351,16 +357,19 @@ cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk,
 }
 
 // Evaluation key in the keyswitch basis, NTT domain, with Shoup companions:
-// d_evk [ell][k][N] of (value, floor(value 2^32 / p)). Synchronous.
+// d_evk [ell][k][N] of (value, floor(value 2^32 / p)); at N = ROWS_N a second
+// copy laid out by lane follows it (the 64-coefficient keyswitch reads that
+// one). Synchronous.
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk) {
     const int k = relin.h.k;
     const size_t words = (size_t)ell * k * n;
+    const bool rows = relin.h.logn == ROWS_LOGN;
     uint64_t* d_limbs = nullptr;
     uint32_t* d_res = nullptr;
     uint2* out = nullptr;
     cudaError_t e = cudaMalloc(&d_limbs, sizeof(uint64_t) * (size_t)ell * n * l64);
     if (e == cudaSuccess) e = cudaMalloc(&d_res, sizeof(uint32_t) * words);
-    if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(uint2) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(uint2) * words * (rows ? 2 : 1));
     if (e == cudaSuccess)
         e = cudaMemcpy(d_limbs, h_evk, sizeof(uint64_t) * (size_t)ell * n * l64, cudaMemcpyHostToDevice);
     cy_status st = (e == cudaSuccess) ? CY_OK : cuda_error(e, "evaluation key upload");
@@ -372,6 +381,12 @@ cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n,
         void* args[] = {(void*)&Bd, (void*)&d_res, (void*)&out, (void*)&total};
         st = launch(shoup_pairs_kernel(), "shoup_pairs", relin.h.logn, dim3((unsigned)((total + 255) / 256)), dim3(256),
                     0, 0, args);
+        if (st == CY_OK && rows) {
+            uint2* out_rows = out + words;
+            void* rargs[] = {(void*)&out, (void*)&out_rows, (void*)&total};
+            st = launch(evk_rows_kernel(), "evk_rows", relin.h.logn, dim3((unsigned)((total + 255) / 256)),
+                        dim3(256), 0, 0, rargs);
+        }
     }
     if (st == CY_OK) {
         e = cudaDeviceSynchronize();

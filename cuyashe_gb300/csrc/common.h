@@ -12,6 +12,12 @@ constexpr int LOGN_MAX = 14;      // N <= 16384
 constexpr int NMAX = 1 << LOGN_MAX;
 constexpr int TABLE_PRIMES = 64;  // word-sized NTT primes with device twiddle tables
 constexpr int PRIME_TWO_ADIC = 16;  // every table prime is 1 mod 2^16
+// Length with a 64-coefficients-per-thread schedule (two passes of six stages):
+// its row-pass twiddles have a per-lane table of ROWS_WORDS entries per prime.
+constexpr int ROWS_LOGN = 12;
+constexpr int ROWS_N = 1 << ROWS_LOGN;
+constexpr int ROWS_G = ROWS_N >> 6;       // threads per transform
+constexpr int ROWS_WORDS = 63 * ROWS_G;   // sum over the six stages of 2^l * G
 
 // What the epilogue of a product kernel computes from the recombined integer X
 // (|X| < M/4, M the basis product):
@@ -59,6 +65,10 @@ struct BasisDev {
     uint32_t frac_m[2];         // YASHE: floor((q - R_M) 2^64 / q)
     const uint2* psi[KMAX];     // forward twiddles (w, floor(w 2^32/p)), bit-reversed powers of psi
     const uint2* ipsi[KMAX];    // inverse twiddles
+    // N = ROWS_N only: the twiddles of the row pass of the 64-coefficient schedule,
+    // laid out by lane (ntt_core.cuh, load_twiddle_rows); null for other N
+    const uint2* psi_r[KMAX];
+    const uint2* ipsi_r[KMAX];
 };
 
 // One product of a mixed batch (different N and q per job) for the persistent

@@ -41,7 +41,16 @@ struct PrimeTable {
     std::vector<uint32_t> primes;
     uint2* d_psi = nullptr;   // [TABLE_PRIMES][NMAX]
     uint2* d_ipsi = nullptr;  // [TABLE_PRIMES][NMAX]
+    uint2* d_psi_r = nullptr;   // [TABLE_PRIMES][ROWS_WORDS] row-pass twiddles of N = ROWS_N by lane
+    uint2* d_ipsi_r = nullptr;  // [TABLE_PRIMES][ROWS_WORDS]
 };
+// Entry of the row-pass table of stage l (0..5), twiddle h (< 2^l) and lane tau
+// (< ROWS_G): stage l starts at ROWS_G (2^l - 1); for l >= 1 the pairs (h, h+1)
+// are 16-byte records [h/2][tau].
+inline size_t rows_index(int l, int h, int tau) {
+    const size_t base = (size_t)ROWS_G * ((1u << l) - 1);
+    return l == 0 ? base + tau : base + (size_t)(h >> 1) * 2 * ROWS_G + 2 * (size_t)tau + (h & 1);
+}
 cy_status prime_table(int device, const PrimeTable** out);
 const std::vector<uint32_t>& table_primes();  // host-only, no CUDA
 

@@ -28,6 +28,7 @@ void fill_n12_e4t(KernelSet& ks);
 void fill_n14_e4d1(KernelSet& ks);
 void fill_n12_e4u(KernelSet& ks);
 void fill_n14_pair(KernelSet& ks);
+void fill_n12_e6(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -67,6 +68,7 @@ static const VariantTable& variants() {
         add(12, fill_n12_e4t);
         add(14, fill_n14_e4d1);
         add(12, fill_n12_e4u);
+        add(12, fill_n12_e6);  // 64 coefficients per thread: two passes, one transpose
         {
             KernelSet ks = T.v[14][0];  // the default set's standalone NTT
             fill_n14_pair(ks);
@@ -127,6 +129,18 @@ __global__ void k_shoup_pairs(const BasisDev* __restrict__ B, const uint32_t* __
     const uint32_t p = B->p[prime];
     const uint32_t x = v[idx];
     out[idx] = make_uint2(x, (uint32_t)(((uint64_t)x << 32) / p));
+}
+
+// The copy of an NTT-domain evaluation key [ell][k][ROWS_N] of (value, Shoup)
+// pairs laid out by lane for the row pass of the 64-coefficient schedule: the
+// entry at position 64 tau + u goes to record [u/2][tau], word u mod 2.
+__global__ void k_evk_rows(const uint2* __restrict__ in, uint2* __restrict__ out, long long total) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long row = idx / ROWS_N;
+    const int pos = (int)(idx % ROWS_N);
+    const int tau = pos >> 6, u = pos & 63;
+    out[row * ROWS_N + (u >> 1) * 2 * ROWS_G + 2 * tau + (u & 1)] = in[idx];
 }
 
 // Elementwise c = a +/- b mod q over [count][l64] limbs (inputs in [0, q)).
@@ -200,5 +214,6 @@ void* addsub_kernel(int l64, bool sub) {
 
 void* crt_kernel() { return (void*)k_crt; }
 void* shoup_pairs_kernel() { return (void*)k_shoup_pairs; }
+void* evk_rows_kernel() { return (void*)k_evk_rows; }
 
 }  // namespace cy

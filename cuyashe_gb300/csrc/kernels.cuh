@@ -226,11 +226,11 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
         }
     }
     constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, 2>();
-    int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0);
+    int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
     uint32_t z[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
-    ntt_inverse<PL, 1>(z, ipsi, c.p, tau, smem, STRIDE, buf);
+    ntt_inverse<PL, 1>(z, ipsi, c.p, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];
@@ -304,13 +304,23 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
                 }
             }
         }
-        buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf);
+        buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf, CtaSync(), 1, B->psi_r[prime]);
 #pragma unroll
         for (int o = 0; o < ND; o++) {
             const int d = d0 + o;
             if (d < ell) {
                 const uint2* __restrict__ g = evk + ((size_t)d * k + prime) * PL::N;
-                if constexpr (PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE) {
+                if constexpr (rows_pass<PL, LAST>()) {
+                    // the key's copy laid out by lane (after the [ell][k][N] table): the
+                    // pair (u, u+1) of lane tau is the 16-byte record [u/2][tau]
+                    const uint4* g4 = reinterpret_cast<const uint4*>(g + (size_t)ell * k * PL::N) + tau;
+#pragma unroll
+                    for (int h = 0; h < E / 2; h++) {
+                        const uint4 W = __ldg(g4 + h * PL::G);
+                        acc[0][2 * h] = red(acc[0][2 * h] + shoup(x[o][2 * h], W.x, W.y, p), 2 * p);
+                        acc[0][2 * h + 1] = red(acc[0][2 * h + 1] + shoup(x[o][2 * h + 1], W.z, W.w, p), 2 * p);
+                    }
+                } else if constexpr (PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE) {
                     // after the last pass a thread's E positions are contiguous: 16-byte loads
                     const uint4* g4 = reinterpret_cast<const uint4*>(g + group_base<PL, LAST>(tau, 0));
 #pragma unroll
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
             }
         }
     }
-    ntt_inverse<PL, 1>(acc, ipsi, p, tau, smem, STRIDE, buf);
+    ntt_inverse<PL, 1>(acc, ipsi, p, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = acc[0][e];
@@ -407,6 +417,69 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 #pragma unroll
             for (int e = 0; e < E; e++) v[o][slot_pos<PL, 0>(tau, e)] = red(shoup(x[o][e], w, ws, p), p);
         }
+    }
+}
+
+// --------------------------------------------------------------------------
+// k_ntt1: the same transform, one residue vector per block, for schedules whose
+// threads hold many coefficients (E = 64: 64 threads, two register passes of six
+// stages and one exchange, a transpose through shared memory). Grid (jobs,
+// primes): consecutive blocks share a prime, so the blocks resident on an SM
+// read the same twiddle table (L1 hits).
+// --------------------------------------------------------------------------
+template <int LOGN, int LOGE, bool INV>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+    k_ntt1(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv,
+           int njobs) {
+    using PL = NttPlan<LOGN, LOGE>;
+    constexpr int E = PL::E;
+    constexpr int LAST = PL::NPASS - 1;
+    extern __shared__ uint32_t smem[];
+    const int tau = threadIdx.x;
+    const int job = blockIdx.x;
+    const int prime = blockIdx.y;
+    const int k = B->k;
+    const uint32_t p = B->p[prime];
+    uint32_t* v = res + ((size_t)job * k + prime) * PL::N;
+    uint32_t x[1][E];
+    // one exchange (two passes) needs no barrier ahead of its writes: a second,
+    // never used region offset stands in for the alternation; more passes share
+    // one region with a barrier before each exchange
+    constexpr int STRIDE = PL::NPASS <= 2 ? PL::SMW : 0;
+    constexpr bool VEC = PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE && E % 4 == 0;
+    if (!INV) {
+#pragma unroll
+        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, 0>(tau, e)];
+        ntt_forward<PL, 1>(x, B->psi[prime], p, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
+        if constexpr (VEC) {
+            uint4* d4 = reinterpret_cast<uint4*>(v + group_base<PL, LAST>(tau, 0));
+#pragma unroll
+            for (int h = 0; h < E / 4; h++)
+                d4[h] = make_uint4(red(red(x[0][4 * h], 2 * p), p), red(red(x[0][4 * h + 1], 2 * p), p),
+                                   red(red(x[0][4 * h + 2], 2 * p), p), red(red(x[0][4 * h + 3], 2 * p), p));
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) v[slot_pos<PL, LAST>(tau, e)] = red(red(x[0][e], 2 * p), p);
+        }
+    } else {
+        const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
+        if constexpr (VEC) {
+            const uint4* s4 = reinterpret_cast<const uint4*>(v + group_base<PL, LAST>(tau, 0));
+#pragma unroll
+            for (int h = 0; h < E / 4; h++) {
+                const uint4 q4 = s4[h];
+                x[0][4 * h] = q4.x;
+                x[0][4 * h + 1] = q4.y;
+                x[0][4 * h + 2] = q4.z;
+                x[0][4 * h + 3] = q4.w;
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
+        }
+        ntt_inverse<PL, 1>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0, CtaSync(), 1, B->ipsi_r[prime]);
+#pragma unroll
+        for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
     }
 }
 
@@ -931,26 +1004,36 @@ void fill_l64(KernelSet& ks) {
 // ND_LO: digits per pass of the keyswitch kernel used when four do not fit (2, or 1
 // for fewer registers); ND_HI: digits per pass of the one used when the digit
 // count is a multiple of four and it fits (4, or 2 for fewer registers).
+// SPEC_MASK: the limb counts (bit L64) that get specialised kernels when
+// SPECIALISE is set.
 template <int LOGN, int LOGE, bool SPECIALISE, int MB_MUL = 0, int MB_KS = 0, bool SINGLE_KS = false,
-          bool SINGLE_MUL = false, int ND_LO = 2, int ND_HI = 4>
+          bool SINGLE_MUL = false, int ND_LO = 2, int ND_HI = 4, unsigned SPEC_MASK = 0x4Eu>
 void fill_kernel_set(KernelSet& ks) {
     using PL = NttPlan<LOGN, LOGE>;
     ks.logn = LOGN;
     ks.loge = LOGE;
     ks.threads = PL::G;
     fill_l64<LOGN, LOGE, 0, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
-    if constexpr (SPECIALISE) {
+    if constexpr (SPECIALISE && (SPEC_MASK & 2u))
         fill_l64<LOGN, LOGE, 1, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+    if constexpr (SPECIALISE && (SPEC_MASK & 4u))
         fill_l64<LOGN, LOGE, 2, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+    if constexpr (SPECIALISE && (SPEC_MASK & 8u))
         fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+    if constexpr (SPECIALISE && (SPEC_MASK & 64u))
         fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
+    if constexpr (LOGE >= 6) {  // one transform per block (k_ntt1)
+        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false>;
+        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true>;
+        ks.ntt_jobs_per_block = 1;
+    } else {
+        ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
+        ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
     }
-    ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;
-    ks.ntt[1] = (void*)k_ntt<LOGN, LOGE, true>;
     ks.smem_mul = SINGLE_MUL ? (size_t)2 * PL::SMW * 4 : region_bytes<PL, 2>();
     ks.smem_ks[0] = SINGLE_KS ? (size_t)ND_LO * PL::SMW * 4 : region_bytes<PL, ND_LO>();
     ks.smem_ks[1] = SINGLE_KS ? (size_t)ND_HI * PL::SMW * 4 : region_bytes<PL, ND_HI>();
-    ks.smem_ntt = region_bytes<PL, 2>();
+    ks.smem_ntt = LOGE >= 6 ? (size_t)PL::SMW * 4 : region_bytes<PL, 2>();
 }
 
 }  // namespace cy

@@ -68,14 +68,19 @@ struct GroupSync {
 //   * an XOR of the low 5 bits with bits of the row (pos >> 5) when both sides
 //     are strided (LOGD = R and 0), which permutes words inside each 32-word row.
 // Every layout is a bijection into SMW = N + N/2^R words.
+// With R = 6 (64 coefficients per thread) one word is added after every 64:
+// the side with LOGD = 0 then reads 64 consecutive positions per thread at a
+// stride of 65 words between lanes (all banks distinct), and the side whose
+// lanes hold consecutive positions stays conflict free.
 template <int R, int DA, int DB>
 struct XLayout {
     static constexpr int DMIN = DA < DB ? DA : DB;
     static constexpr int DMAX = DA < DB ? DB : DA;
     static constexpr bool SWZ = DMAX < 5 && (R == 3 || R == 4);
     static constexpr int PAD = (DMIN >= 5 || DMIN == 0 || DMIN != R || R >= 5) ? 1 : (1 << (5 - R));
-    // the padded word of a position whose bits below 5 and above are independent
-    __host__ __device__ static constexpr int pad(int pos) { return pos + PAD * (pos >> 5); }
+    static constexpr int PSH = R >= 6 ? 6 : 5;  // padding period 2^PSH words
+    // the padded word of a position whose bits below PSH and above are independent
+    __host__ __device__ static constexpr int pad(int pos) { return pos + PAD * (pos >> PSH); }
     __device__ __forceinline__ static int swz(int pos) {
         const int x = pos >> 5;
         if constexpr (R == 3) return pos ^ (x & 7) ^ (((x >> 1) & 3) << 3);
@@ -109,15 +114,35 @@ __device__ __forceinline__ uint2 load_twiddle(const uint2* __restrict__ twl, int
     return (h & 1) ? make_uint2(W2.z, W2.w) : make_uint2(W2.x, W2.y);
 }
 
+// Plans with 64 coefficients per thread end (forward) or start (inverse) with a
+// pass in which thread tau owns the 64 consecutive positions of row tau, and
+// needs twiddles tw[2^(S0+l) + tau 2^l + h] (h < 2^l): 2^l consecutive entries
+// per thread, 512 bytes apart between lanes at l = 6. Those passes read a copy
+// of the table laid out by lane ("rows" table, one per prime and length):
+// stage l starts at entry G (2^l - 1); its twiddle pairs (h, h+1) are 16-byte
+// records [h/2][tau], so that a warp's load covers 512 consecutive bytes.
+template <class PL, int PASS>
+__host__ __device__ constexpr bool rows_pass() {
+    return PL::LOGE == 6 && PASS == PL::NPASS - 1 && PL::LOGD(PASS) == 0;
+}
+__device__ __forceinline__ uint2 load_twiddle_rows(const uint2* __restrict__ twl, int h, int l, int G) {
+    if (l == 0) return __ldg(twl);
+    const uint4 W2 = __ldg(reinterpret_cast<const uint4*>(twl + (h >> 1) * 2 * G));
+    return (h & 1) ? make_uint2(W2.z, W2.w) : make_uint2(W2.x, W2.y);
+}
+
 // tm: twiddle-offset multiplier. A transform of length N is stages 0.. of one of
 // length 2N restricted to half h of it when its stage-s twiddles start at
 // (2 + h) * 2^s instead of 2^s (tm = 2 + h); tm = 1 for a whole transform.
+// twr: the rows table of this prime and length (plans with 64 coefficients per
+// thread; unused otherwise).
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                         int tau, int tm = 1) {
+                                         int tau, int tm = 1, const uint2* __restrict__ twr = nullptr) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
     constexpr int NV = PL::E >> R;
+    constexpr bool ROWS = rows_pass<PL, PASS>();
 #pragma unroll
     for (int v = 0; v < NV; v++) {
         const int gam = tau + (v << (PL::LOGN - PL::LOGE));
@@ -125,16 +150,19 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = 0; l < R; l++) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            const uint2* twl = ROWS ? twr + PL::G * ((1 << l) - 1) + (l == 0 ? tau : 2 * tau)
+                                    : tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            // one flat loop of 2^(R-1) butterflies per stage (a trip count that does
+            // not depend on l, so that every loop unrolls fully for R = 6 too):
+            // butterfly b is j = b mod half of twiddle group h = b / half
+            uint2 W = make_uint2(0u, 0u);
 #pragma unroll
-            for (int h = 0; h < (1 << l); h++) {
-                const uint2 W = load_twiddle(twl, h, l);
+            for (int b = 0; b < GS / 2; b++) {
+                const int h = b >> (R - 1 - l), j = b & (half - 1);
+                if (j == 0) W = ROWS ? load_twiddle_rows(twl, h, l, PL::G) : load_twiddle(twl, h, l);
+                const int u = (h << (R - l)) + j;
 #pragma unroll
-                for (int j = 0; j < half; j++) {
-                    const int u = (h << (R - l)) + j;
-#pragma unroll
-                    for (int o = 0; o < NOPS; o++) ct_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
-                }
+                for (int o = 0; o < NOPS; o++) ct_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
             }
         }
     }
@@ -142,10 +170,11 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
-                                         int tau, int tm = 1) {
+                                         int tau, int tm = 1, const uint2* __restrict__ twr = nullptr) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
     constexpr int NV = PL::E >> R;
+    constexpr bool ROWS = rows_pass<PL, PASS>();
 #pragma unroll
     for (int v = 0; v < NV; v++) {
         const int gam = tau + (v << (PL::LOGN - PL::LOGE));
@@ -153,16 +182,16 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
 #pragma unroll
         for (int l = R - 1; l >= 0; l--) {
             const int half = 1 << (R - 1 - l);
-            const uint2* twl = tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            const uint2* twl = ROWS ? twr + PL::G * ((1 << l) - 1) + (l == 0 ? tau : 2 * tau)
+                                    : tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
+            uint2 W = make_uint2(0u, 0u);
 #pragma unroll
-            for (int h = 0; h < (1 << l); h++) {
-                const uint2 W = load_twiddle(twl, h, l);
+            for (int b = 0; b < GS / 2; b++) {  // as in fwd_pass
+                const int h = b >> (R - 1 - l), j = b & (half - 1);
+                if (j == 0) W = ROWS ? load_twiddle_rows(twl, h, l, PL::G) : load_twiddle(twl, h, l);
+                const int u = (h << (R - l)) + j;
 #pragma unroll
-                for (int j = 0; j < half; j++) {
-                    const int u = (h << (R - l)) + j;
-#pragma unroll
-                    for (int o = 0; o < NOPS; o++) gs_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
-                }
+                for (int o = 0; o < NOPS; o++) gs_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
             }
         }
     }
@@ -213,13 +242,13 @@ template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct FwdFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
                                               uint32_t p, int tau, uint32_t* sm, int stride, int buf,
-                                              Sync bar = Sync(), int tm = 1) {
+                                              Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr) {
         if constexpr (PASS >= PL::NPASS) {
             return buf;
         } else {
             exchange<PL, PASS - 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau, tm);
-            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm);
+            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau, tm, twr);
+            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm, twr);
         }
     }
 };
@@ -229,13 +258,13 @@ template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct InvFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
                                               uint32_t p, int tau, uint32_t* sm, int stride, int buf,
-                                              Sync bar = Sync(), int tm = 1) {
+                                              Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr) {
         if constexpr (PASS < 0) {
             return buf;
         } else {
             exchange<PL, PASS + 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            inv_pass<PL, PASS, NOPS>(x, tw, p, tau, tm);
-            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm);
+            inv_pass<PL, PASS, NOPS>(x, tw, p, tau, tm, twr);
+            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm, twr);
         }
     }
 };
@@ -245,18 +274,18 @@ struct InvFrom {
 template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
                                            int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
-                                           int tm = 1) {
-    fwd_pass<PL, 0, NOPS>(x, tw, p, tau, tm);
-    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm);
+                                           int tm = 1, const uint2* __restrict__ twr = nullptr) {
+    fwd_pass<PL, 0, NOPS>(x, tw, p, tau, tm, twr);
+    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm, twr);
 }
 
 // Full inverse transform: registers in last-pass layout -> pass-0 layout.
 template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
                                            int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
-                                           int tm = 1) {
-    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau, tm);
-    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm);
+                                           int tm = 1, const uint2* __restrict__ twr = nullptr) {
+    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau, tm, twr);
+    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm, twr);
 }
 
 }  // namespace cy

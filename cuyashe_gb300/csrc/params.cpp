@@ -124,17 +124,36 @@ cy_status prime_table(int device, const PrimeTable** out) {
             ipsi[(size_t)i * NMAX + j] = make_uint2(wi, shoup_of(wi, p));
         }
     }
+    // row-pass tables of N = ROWS_N: entry (l, h, tau) = tw[2^(S0+l) + tau 2^l + h]
+    // with S0 = ROWS_LOGN - 6 the first stage of the row pass
+    std::vector<uint2> psi_r((size_t)TABLE_PRIMES * ROWS_WORDS), ipsi_r((size_t)TABLE_PRIMES * ROWS_WORDS);
+    for (int i = 0; i < TABLE_PRIMES; i++)
+        for (int l = 0; l < 6; l++)
+            for (int h = 0; h < (1 << l); h++)
+                for (int tau = 0; tau < ROWS_G; tau++) {
+                    const size_t src = (size_t)i * NMAX + ((size_t)1 << (ROWS_LOGN - 6 + l)) + ((size_t)tau << l) + h;
+                    const size_t dst = (size_t)i * ROWS_WORDS + rows_index(l, h, tau);
+                    psi_r[dst] = psi[src];
+                    ipsi_r[dst] = ipsi[src];
+                }
     PrimeTable* t = new PrimeTable();
     t->device = device;
     t->primes = primes;
     const size_t bytes = sizeof(uint2) * (size_t)TABLE_PRIMES * NMAX;
+    const size_t rbytes = sizeof(uint2) * psi_r.size();
     cudaError_t e = cudaMalloc(&t->d_psi, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&t->d_ipsi, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_psi_r, rbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_ipsi_r, rbytes);
     if (e == cudaSuccess) e = cudaMemcpy(t->d_psi, psi.data(), bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(t->d_ipsi, ipsi.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_psi_r, psi_r.data(), rbytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_ipsi_r, ipsi_r.data(), rbytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(t->d_psi);
         cudaFree(t->d_ipsi);
+        cudaFree(t->d_psi_r);
+        cudaFree(t->d_ipsi_r);
         delete t;
         return cuda_error(e, "prime table upload");
     }
@@ -246,6 +265,10 @@ cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, c
     for (int i = 0; i < b.h.k; i++) {
         b.h.psi[i] = tab->d_psi + (size_t)i * NMAX;
         b.h.ipsi[i] = tab->d_ipsi + (size_t)i * NMAX;
+        if (b.h.logn == ROWS_LOGN) {
+            b.h.psi_r[i] = tab->d_psi_r + (size_t)i * ROWS_WORDS;
+            b.h.ipsi_r[i] = tab->d_ipsi_r + (size_t)i * ROWS_WORDS;
+        }
     }
     std::vector<uint32_t> ninv(2 * (size_t)b.h.k);
     for (int i = 0; i < b.h.k; i++) {
