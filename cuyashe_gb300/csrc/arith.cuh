@@ -32,21 +32,40 @@ __device__ __forceinline__ uint32_t mont(uint32_t a, uint32_t b, uint32_t p, uin
     return (uint32_t)(u >> 32);
 }
 
+// The modulus with the constants derived from it. Each field is loaded from
+// memory on its own (BasisDev::p, p2, np, np2), so that the compiler cannot
+// relate them: it then emits the lazy reduction min(x, x - 2p) as one
+// add-then-min and x w - q p as one multiply-add with -p. Constants it can
+// derive from p were measured to cost two more integer instructions per
+// butterfly (8 instead of 6).
+struct Mod {
+    uint32_t p, p2, np, np2;  // p, 2p, -p, -2p (mod 2^32)
+};
+
+// The same constants computed from p in registers: the compiler folds them
+// (fewer live registers, two more instructions per butterfly), for kernels that
+// are short of registers.
+__device__ __forceinline__ Mod mod_of(uint32_t p) { return Mod{p, 2 * p, 0u - p, 0u - 2 * p}; }
+
+// x * w mod p in [0, 2p), any 32-bit x (Shoup, with -p from m)
+__device__ __forceinline__ uint32_t shoup_m(uint32_t x, uint32_t w, uint32_t ws, const Mod& m) {
+    return __umulhi(x, ws) * m.np + x * w;
+}
+
 // Cooley-Tukey butterfly (Harvey's lazy form): X, Y in [0, 4p) -> X + wY, X - wY in [0, 4p).
-__device__ __forceinline__ void ct_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, uint32_t p) {
-    const uint32_t p2 = 2 * p;
-    const uint32_t x = red(X, p2);
-    const uint32_t t = shoup(Y, w, ws, p);
-    Y = x - t + p2;
+// Six integer instructions: add-then-min, mul.hi, two multiply-adds, two adds.
+__device__ __forceinline__ void ct_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, const Mod& m) {
+    const uint32_t x = __viaddmin_u32(X, m.np2, X);  // [0, 2p)
+    const uint32_t t = shoup_m(Y, w, ws, m);        // [0, 2p)
+    Y = x - t + m.p2;
     X = x + t;
 }
 
 // Gentleman-Sande butterfly: X, Y in [0, 2p) -> X + Y, (X - Y) w in [0, 2p).
-__device__ __forceinline__ void gs_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, uint32_t p) {
-    const uint32_t p2 = 2 * p;
-    const uint32_t s = red(X + Y, p2);  // one add, one add-then-min
-    const uint32_t d = X - Y + p2;
-    Y = shoup(d, w, ws, p);
+__device__ __forceinline__ void gs_bfly(uint32_t& X, uint32_t& Y, uint32_t w, uint32_t ws, const Mod& m) {
+    const uint32_t s = __viaddmin_u32(X, Y, X + Y + m.np2);  // min(X + Y, X + Y - 2p)
+    const uint32_t d = X - Y + m.p2;
+    Y = shoup_m(d, w, ws, m);
     X = s;
 }
 

@@ -52,6 +52,7 @@ struct BasisDev {
     uint32_t B0[L32MAX];       // MODQ: ((-M) mod q) << s        YASHE: ((-I_M) mod q) << s
     uint32_t B1[L32MAX];       //                                YASHE: (q - R_M) << s
     uint32_t p[KMAX];
+    uint32_t p2[KMAX], np[KMAX], np2[KMAX];  // 2p, -p, -2p (mod 2^32), read apart from p (arith.cuh, Mod)
     uint32_t pinv[KMAX];       // -p^-1 mod 2^32
     uint32_t ycon[KMAX];       // residue -> [X * Mhat_i^-1]_{p_i} factor (N^-1, Montgomery folded)
     uint32_t ycon_sh[KMAX];    // Shoup companion of ycon

@@ -62,11 +62,12 @@ __device__ __forceinline__ void mixed_ntt_unit(const MixedJob& J, const MixedUni
             x[1][e] = crt_coef<false>(J.b, pos, J.l64, crt, nullptr, c);
         }
     }
-    int buf = ntt_forward<PL, 2, GroupSync>(x, B->psi[prime], c.p, tau, sm, STRIDE, 0, bar);
+    const Mod m = mod_of(c.p);  // 64 registers per thread: constants folded
+    int buf = ntt_forward<PL, 2, GroupSync>(x, B->psi[prime], m, tau, sm, STRIDE, 0, bar);
     uint32_t z[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
-    ntt_inverse<PL, 1, GroupSync>(z, B->ipsi[prime], c.p, tau, sm, STRIDE, buf, bar);
+    ntt_inverse<PL, 1, GroupSync>(z, B->ipsi[prime], m, tau, sm, STRIDE, buf, bar);
     uint32_t* out = J.resid + (size_t)prime * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];

@@ -36,14 +36,31 @@ __host__ __device__ constexpr size_t region_bytes() {
     return (size_t)(region_stride<PL, NOPS>() ? 2 : 1) * NOPS * PL::SMW * 4;
 }
 
+// The modulus of prime i with its derived constants, each read on its own.
+__device__ __forceinline__ Mod load_mod(const BasisDev* __restrict__ B, int i) {
+    Mod m;
+    m.p = B->p[i];
+    m.p2 = B->p2[i];
+    m.np = B->np[i];
+    m.np2 = B->np2[i];
+    return m;
+}
+
+// a + b reduced from [0, 4p) to [0, 2p) (a, b in [0, 2p)): one add, one add-then-min
+__device__ __forceinline__ uint32_t mac_red(uint32_t a, uint32_t b, const Mod& m) {
+    return __viaddmin_u32(a, b, a + b + m.np2);
+}
+
 // Per-prime constants a product kernel keeps in registers.
 struct PrimeCtx {
     uint32_t p, pinv, r32, r32_sh, one_sh, qmodp;
+    Mod m;
 };
 
 __device__ __forceinline__ PrimeCtx load_prime_ctx(const BasisDev* __restrict__ B, int i) {
     PrimeCtx c;
-    c.p = B->p[i];
+    c.m = load_mod(B, i);
+    c.p = c.m.p;
     c.pinv = B->pinv[i];
     c.r32 = B->r32[i];
     c.r32_sh = B->r32_sh[i];
@@ -226,11 +243,11 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
         }
     }
     constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, 2>();
-    int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
+    int buf = ntt_forward<PL, 2>(x, psi, c.m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
     uint32_t z[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
-    ntt_inverse<PL, 1>(z, ipsi, c.p, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
+    ntt_inverse<PL, 1>(z, ipsi, c.m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];
@@ -255,7 +272,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
     const int prime = blockIdx.x;
     const int job = blockIdx.y;
     const int k = B->k, l64 = L64 > 0 ? L64 : B->l64;
-    const uint32_t p = B->p[prime];
+    const Mod m = load_mod(B, prime);
+    const uint32_t p = m.p;
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
     const uint64_t* cj = C + (size_t)job * PL::N * l64;
@@ -304,7 +322,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
                 }
             }
         }
-        buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf, CtaSync(), 1, B->psi_r[prime]);
+        buf = ntt_forward<PL, ND>(x, psi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->psi_r[prime]);
 #pragma unroll
         for (int o = 0; o < ND; o++) {
             const int d = d0 + o;
@@ -317,8 +335,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
 #pragma unroll
                     for (int h = 0; h < E / 2; h++) {
                         const uint4 W = __ldg(g4 + h * PL::G);
-                        acc[0][2 * h] = red(acc[0][2 * h] + shoup(x[o][2 * h], W.x, W.y, p), 2 * p);
-                        acc[0][2 * h + 1] = red(acc[0][2 * h + 1] + shoup(x[o][2 * h + 1], W.z, W.w, p), 2 * p);
+                        acc[0][2 * h] = mac_red(acc[0][2 * h], shoup_m(x[o][2 * h], W.x, W.y, m), m);
+                        acc[0][2 * h + 1] = mac_red(acc[0][2 * h + 1], shoup_m(x[o][2 * h + 1], W.z, W.w, m), m);
                     }
                 } else if constexpr (PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE) {
                     // after the last pass a thread's E positions are contiguous: 16-byte loads
@@ -326,20 +344,20 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
 #pragma unroll
                     for (int h = 0; h < E / 2; h++) {
                         const uint4 W = __ldg(g4 + h);
-                        acc[0][2 * h] = red(acc[0][2 * h] + shoup(x[o][2 * h], W.x, W.y, p), 2 * p);
-                        acc[0][2 * h + 1] = red(acc[0][2 * h + 1] + shoup(x[o][2 * h + 1], W.z, W.w, p), 2 * p);
+                        acc[0][2 * h] = mac_red(acc[0][2 * h], shoup_m(x[o][2 * h], W.x, W.y, m), m);
+                        acc[0][2 * h + 1] = mac_red(acc[0][2 * h + 1], shoup_m(x[o][2 * h + 1], W.z, W.w, m), m);
                     }
                 } else {
 #pragma unroll
                     for (int e = 0; e < E; e++) {
                         const uint2 W = __ldg(g + slot_pos<PL, LAST>(tau, e));
-                        acc[0][e] = red(acc[0][e] + shoup(x[o][e], W.x, W.y, p), 2 * p);
+                        acc[0][e] = mac_red(acc[0][e], shoup_m(x[o][e], W.x, W.y, m), m);
                     }
                 }
             }
         }
     }
-    ntt_inverse<PL, 1>(acc, ipsi, p, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
+    ntt_inverse<PL, 1>(acc, ipsi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = acc[0][e];
@@ -365,7 +383,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
     const int job0 = 2 * blockIdx.y;
     const bool two = job0 + 1 < njobs;
     const int k = B->k;
-    const uint32_t p = B->p[prime];
+    const Mod m = load_mod(B, prime);
+    const uint32_t p = m.p;
     uint32_t* v[2] = {res + ((size_t)job0 * k + prime) * PL::N, res + ((size_t)(two ? job0 + 1 : job0) * k + prime) * PL::N};
     uint32_t x[2][E];
     constexpr int STRIDE = region_stride<PL, 2>();
@@ -376,7 +395,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
         for (int o = 0; o < 2; o++)
 #pragma unroll
             for (int e = 0; e < E; e++) x[o][e] = v[o][slot_pos<PL, 0>(tau, e)];
-        ntt_forward<PL, 2>(x, B->psi[prime], p, tau, smem, STRIDE, 0);
+        ntt_forward<PL, 2>(x, B->psi[prime], m, tau, smem, STRIDE, 0);
 #pragma unroll
         for (int o = 0; o < 2; o++) {
             if (o == 1 && !two) break;
@@ -410,7 +429,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
                 for (int e = 0; e < E; e++) x[o][e] = v[o][slot_pos<PL, LAST>(tau, e)];
             }
         }
-        ntt_inverse<PL, 2>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0);
+        ntt_inverse<PL, 2>(x, B->ipsi[prime], m, tau, smem, STRIDE, 0);
 #pragma unroll
         for (int o = 0; o < 2; o++) {
             if (o == 1 && !two) break;
@@ -426,20 +445,35 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 // stages and one exchange, a transpose through shared memory). Grid (jobs,
 // primes): consecutive blocks share a prime, so the blocks resident on an SM
 // read the same twiddle table (L1 hits).
+// MINB > 0: blocks per SM the kernel is compiled for.
+// COAL (two passes of six stages): the row side of the transform (forward
+// output, inverse input) goes through the exchange region once more, so that
+// every global access of a warp covers 128 consecutive bytes instead of 32
+// rows 256 bytes apart.
+// TPB: transforms per block (TPB groups of G threads, one exchange region each,
+// block-wide barriers). Several transforms in step keep the warps of an SM on
+// nearby instructions (the unrolled transform is larger than the instruction
+// cache). Jobs past the last are computed on the last job and not stored.
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, bool INV>
-__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
+template <int LOGN, int LOGE, bool INV, int MINB = 0, bool COAL = false, int TPB = 1>
+__global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB : 1))
     k_ntt1(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv,
            int njobs) {
     using PL = NttPlan<LOGN, LOGE>;
     constexpr int E = PL::E;
     constexpr int LAST = PL::NPASS - 1;
-    extern __shared__ uint32_t smem[];
-    const int tau = threadIdx.x;
-    const int job = blockIdx.x;
+    static_assert(!COAL || (PL::NPASS == 2 && LOGE == 6 && LOGN == 12), "row-side staging: N = 4096, E = 64");
+    extern __shared__ uint32_t smem_all[];
+    const int sub = TPB > 1 ? (int)threadIdx.x / PL::G : 0;
+    const int tau = TPB > 1 ? (int)threadIdx.x % PL::G : (int)threadIdx.x;
+    uint32_t* smem = smem_all + sub * PL::SMW;
+    const int job_raw = blockIdx.x * TPB + sub;
+    const bool store = job_raw < njobs;
+    const int job = store ? job_raw : njobs - 1;
     const int prime = blockIdx.y;
     const int k = B->k;
-    const uint32_t p = B->p[prime];
+    const Mod m = load_mod(B, prime);
+    const uint32_t p = m.p;
     uint32_t* v = res + ((size_t)job * k + prime) * PL::N;
     uint32_t x[1][E];
     // one exchange (two passes) needs no barrier ahead of its writes: a second,
@@ -450,20 +484,43 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
     if (!INV) {
 #pragma unroll
         for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, 0>(tau, e)];
-        ntt_forward<PL, 1>(x, B->psi[prime], p, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
-        if constexpr (VEC) {
-            uint4* d4 = reinterpret_cast<uint4*>(v + group_base<PL, LAST>(tau, 0));
+        ntt_forward<PL, 1>(x, B->psi[prime], m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
+        if constexpr (COAL) {
+            // row tau (positions 64 tau + u) into the padded region (word 65 tau + u),
+            // then column tau (positions tau + 64 m, word 65 m + tau) to global memory
+            __syncthreads();
 #pragma unroll
-            for (int h = 0; h < E / 4; h++)
-                d4[h] = make_uint4(red(red(x[0][4 * h], 2 * p), p), red(red(x[0][4 * h + 1], 2 * p), p),
-                                   red(red(x[0][4 * h + 2], 2 * p), p), red(red(x[0][4 * h + 3], 2 * p), p));
-        } else {
+            for (int u = 0; u < E; u++) smem[65 * tau + u] = red(red(x[0][u], 2 * p), p);
+            __syncthreads();
+            if (store) {
+#pragma unroll
+                for (int m = 0; m < E; m++) v[tau + 64 * m] = smem[tau + 65 * m];
+            }
+        } else if constexpr (VEC) {
+            if (store) {
+                uint4* d4 = reinterpret_cast<uint4*>(v + group_base<PL, LAST>(tau, 0));
+#pragma unroll
+                for (int h = 0; h < E / 4; h++)
+                    d4[h] = make_uint4(red(red(x[0][4 * h], 2 * p), p), red(red(x[0][4 * h + 1], 2 * p), p),
+                                       red(red(x[0][4 * h + 2], 2 * p), p), red(red(x[0][4 * h + 3], 2 * p), p));
+            }
+        } else if (store) {
 #pragma unroll
             for (int e = 0; e < E; e++) v[slot_pos<PL, LAST>(tau, e)] = red(red(x[0][e], 2 * p), p);
         }
     } else {
         const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
-        if constexpr (VEC) {
+        int stride = STRIDE;
+        if constexpr (COAL) {
+            // columns in (coalesced), rows out of the padded region; the exchange
+            // of the inverse then reuses the region after a barrier (stride 0)
+#pragma unroll
+            for (int m = 0; m < E; m++) smem[tau + 65 * m] = v[tau + 64 * m];
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < E; u++) x[0][u] = smem[65 * tau + u];
+            stride = 0;
+        } else if constexpr (VEC) {
             const uint4* s4 = reinterpret_cast<const uint4*>(v + group_base<PL, LAST>(tau, 0));
 #pragma unroll
             for (int h = 0; h < E / 4; h++) {
@@ -477,9 +534,11 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 #pragma unroll
             for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
         }
-        ntt_inverse<PL, 1>(x, B->ipsi[prime], p, tau, smem, STRIDE, 0, CtaSync(), 1, B->ipsi_r[prime]);
+        ntt_inverse<PL, 1>(x, B->ipsi[prime], m, tau, smem, stride, 0, CtaSync(), 1, B->ipsi_r[prime]);
+        if (store) {
 #pragma unroll
-        for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
+            for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
+        }
     }
 }
 
@@ -1022,9 +1081,10 @@ void fill_kernel_set(KernelSet& ks) {
         fill_l64<LOGN, LOGE, 3, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
     if constexpr (SPECIALISE && (SPEC_MASK & 64u))
         fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
-    if constexpr (LOGE >= 6) {  // one transform per block (k_ntt1)
-        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false>;
-        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true>;
+    if constexpr (LOGE >= 6) {  // one transform per block (k_ntt1), coalesced row side at N = 4096
+        constexpr bool COAL = LOGN == 12 && LOGE == 6;
+        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false, 0, COAL>;
+        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true, 0, COAL>;
         ks.ntt_jobs_per_block = 1;
     } else {
         ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;

@@ -130,18 +130,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
         for (int o = 0; o < 2; o++) {
             const uint32_t other = smem[o * kPairHalf + pos];
             uint32_t lo = h ? other : x[o][e], hi = h ? x[o][e] : other;
-            ct_bfly(lo, hi, w0.x, w0.y, c.p);  // first stage of the whole transform
+            ct_bfly(lo, hi, w0.x, w0.y, c.m);  // first stage of the whole transform
             x[o][e] = h ? hi : lo;
         }
     }
     __syncthreads();  // every thread has read region 0 before the first exchange writes it
     constexpr int STRIDE = region_stride<PL, 2>();
     const int tm = 2 + (int)h;
-    int buf = ntt_forward<PL, 2>(x, psi, c.p, tau, smem, STRIDE, 0, CtaSync(), tm);
+    int buf = ntt_forward<PL, 2>(x, psi, c.m, tau, smem, STRIDE, 0, CtaSync(), tm);
     uint32_t z[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
-    ntt_inverse<PL, 1>(z, ipsi, c.p, tau, smem, STRIDE, buf, CtaSync(), tm);
+    ntt_inverse<PL, 1>(z, ipsi, c.m, tau, smem, STRIDE, buf, CtaSync(), tm);
     pair_finish(z, recv, h, tau, c.p, __ldg(ipsi + 1), resid + ((size_t)job * k + prime) * (2 * kPairHalf));
 }
 
@@ -160,7 +160,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
     const int prime = blockIdx.x >> 1;
     const int job = blockIdx.y;
     const int k = B->k, l64 = L64 > 0 ? L64 : B->l64;
-    const uint32_t p = B->p[prime];
+    const Mod m = load_mod(B, prime);
+    const uint32_t p = m.p;
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
     const uint64_t* cj = C + (size_t)job * (2 * kPairHalf) * l64;
@@ -192,11 +193,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
                 }
                 lo[o] = red(wl, 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
                 hi[o] = red(wh, 2 * p);
-                ct_bfly(lo[o], hi[o], w0.x, w0.y, p);  // first stage of the whole transform
+                ct_bfly(lo[o], hi[o], w0.x, w0.y, m);  // first stage of the whole transform
                 x[o][e] = h ? hi[o] : lo[o];
             }
         }
-        buf = ntt_forward<PL, ND>(x, psi, p, tau, smem, STRIDE, buf, CtaSync(), tm);
+        buf = ntt_forward<PL, ND>(x, psi, m, tau, smem, STRIDE, buf, CtaSync(), tm);
 #pragma unroll
         for (int o = 0; o < ND; o++) {
             const int d = d0 + o;
@@ -206,13 +207,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
 #pragma unroll
                 for (int q = 0; q < E / 2; q++) {
                     const uint4 W = __ldg(g4 + q);
-                    acc[0][2 * q] = red(acc[0][2 * q] + shoup(x[o][2 * q], W.x, W.y, p), 2 * p);
-                    acc[0][2 * q + 1] = red(acc[0][2 * q + 1] + shoup(x[o][2 * q + 1], W.z, W.w, p), 2 * p);
+                    acc[0][2 * q] = mac_red(acc[0][2 * q], shoup_m(x[o][2 * q], W.x, W.y, m), m);
+                    acc[0][2 * q + 1] = mac_red(acc[0][2 * q + 1], shoup_m(x[o][2 * q + 1], W.z, W.w, m), m);
                 }
             }
         }
     }
-    ntt_inverse<PL, 1>(acc, ipsi, p, tau, smem, STRIDE, buf, CtaSync(), tm);
+    ntt_inverse<PL, 1>(acc, ipsi, m, tau, smem, STRIDE, buf, CtaSync(), tm);
     pair_finish(acc, recv, h, tau, p, __ldg(ipsi + 1), resid + ((size_t)job * k + prime) * (2 * kPairHalf));
 }
 

@@ -137,7 +137,7 @@ __device__ __forceinline__ uint2 load_twiddle_rows(const uint2* __restrict__ twl
 // twr: the rows table of this prime and length (plans with 64 coefficients per
 // thread; unused otherwise).
 template <class PL, int PASS, int NOPS>
-__device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+__device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
                                          int tau, int tm = 1, const uint2* __restrict__ twr = nullptr) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
@@ -162,14 +162,14 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
                 if (j == 0) W = ROWS ? load_twiddle_rows(twl, h, l, PL::G) : load_twiddle(twl, h, l);
                 const int u = (h << (R - l)) + j;
 #pragma unroll
-                for (int o = 0; o < NOPS; o++) ct_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
+                for (int o = 0; o < NOPS; o++) ct_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, m);
             }
         }
     }
 }
 
 template <class PL, int PASS, int NOPS>
-__device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+__device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
                                          int tau, int tm = 1, const uint2* __restrict__ twr = nullptr) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
@@ -191,7 +191,7 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
                 if (j == 0) W = ROWS ? load_twiddle_rows(twl, h, l, PL::G) : load_twiddle(twl, h, l);
                 const int u = (h << (R - l)) + j;
 #pragma unroll
-                for (int o = 0; o < NOPS; o++) gs_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, p);
+                for (int o = 0; o < NOPS; o++) gs_bfly(x[o][v * GS + u], x[o][v * GS + u + half], W.x, W.y, m);
             }
         }
     }
@@ -241,14 +241,14 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NOPS][PL::E], uint32_t* s
 template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct FwdFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
-                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf,
+                                              const Mod& m, int tau, uint32_t* sm, int stride, int buf,
                                               Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr) {
         if constexpr (PASS >= PL::NPASS) {
             return buf;
         } else {
             exchange<PL, PASS - 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            fwd_pass<PL, PASS, NOPS>(x, tw, p, tau, tm, twr);
-            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm, twr);
+            fwd_pass<PL, PASS, NOPS>(x, tw, m, tau, tm, twr);
+            return FwdFrom<PL, PASS + 1, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf + 1, bar, tm, twr);
         }
     }
 };
@@ -257,14 +257,14 @@ struct FwdFrom {
 template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct InvFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
-                                              uint32_t p, int tau, uint32_t* sm, int stride, int buf,
+                                              const Mod& m, int tau, uint32_t* sm, int stride, int buf,
                                               Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr) {
         if constexpr (PASS < 0) {
             return buf;
         } else {
             exchange<PL, PASS + 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            inv_pass<PL, PASS, NOPS>(x, tw, p, tau, tm, twr);
-            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf + 1, bar, tm, twr);
+            inv_pass<PL, PASS, NOPS>(x, tw, m, tau, tm, twr);
+            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf + 1, bar, tm, twr);
         }
     }
 };
@@ -272,20 +272,20 @@ struct InvFrom {
 // Full forward transform: registers in pass-0 layout (natural order) ->
 // registers in last-pass layout (bit-reversed order).
 template <class PL, int NOPS, class Sync = CtaSync>
-__device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+__device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
                                            int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
                                            int tm = 1, const uint2* __restrict__ twr = nullptr) {
-    fwd_pass<PL, 0, NOPS>(x, tw, p, tau, tm, twr);
-    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm, twr);
+    fwd_pass<PL, 0, NOPS>(x, tw, m, tau, tm, twr);
+    return FwdFrom<PL, 1, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf, bar, tm, twr);
 }
 
 // Full inverse transform: registers in last-pass layout -> pass-0 layout.
 template <class PL, int NOPS, class Sync = CtaSync>
-__device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, uint32_t p,
+__device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
                                            int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
                                            int tm = 1, const uint2* __restrict__ twr = nullptr) {
-    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, p, tau, tm, twr);
-    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, p, tau, sm, stride, buf, bar, tm, twr);
+    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, m, tau, tm, twr);
+    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf, bar, tm, twr);
 }
 
 }  // namespace cy

@@ -216,6 +216,9 @@ cy_status basis_constants(BasisDev& h, int* crt_bits, int n, const BigUInt& q, i
     for (int i = 0; i < k; i++) {
         const uint32_t p = primes[i];
         h.p[i] = p;
+        h.p2[i] = 2 * p;
+        h.np[i] = 0u - p;
+        h.np2[i] = 0u - 2 * p;
         // -p^-1 mod 2^32 by Newton iteration
         uint32_t inv = p;
         for (int it = 0; it < 5; it++) inv *= 2u - p * inv;
