@@ -58,7 +58,7 @@ const std::vector<uint32_t>& table_primes();  // host-only, no CUDA
 struct Basis {
     BasisDev h{};
     BasisDev* d = nullptr;
-    uint32_t* d_ninv = nullptr;  // [k][2]: N^-1 mod p_i and its Shoup companion
+    uint32_t* d_ninv = nullptr;  // [k][4]: N^-1 mod p_i, N^-1 psi_i^-(NMAX/2), each with its Shoup companion
     int crt_bits = 0;
     const EpiSpecial* epi = nullptr;     // specialised epilogue of this basis, if any
     std::vector<unsigned char> epi_param;  // its parameter block (constants by value)

@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
             }
         }
     } else {
-        const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
+        const uint32_t w = ninv[4 * prime], ws = ninv[4 * prime + 1];
 #pragma unroll
         for (int o = 0; o < 2; o++) {
             if constexpr (VEC) {
@@ -509,7 +509,6 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
             for (int e = 0; e < E; e++) v[slot_pos<PL, LAST>(tau, e)] = red(red(x[0][e], 2 * p), p);
         }
     } else {
-        const uint32_t w = ninv[2 * prime], ws = ninv[2 * prime + 1];
         int stride = STRIDE;
         if constexpr (COAL) {
             // columns in (coalesced), rows out of the padded region; the exchange
@@ -534,10 +533,12 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
 #pragma unroll
             for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
         }
-        ntt_inverse<PL, 1>(x, B->ipsi[prime], m, tau, smem, stride, 0, CtaSync(), 1, B->ipsi_r[prime]);
+        // N^-1 is applied inside the last stage (outputs in [0, p))
+        ntt_inverse<PL, 1>(x, B->ipsi[prime], m, tau, smem, stride, 0, CtaSync(), 1, B->ipsi_r[prime],
+                           ninv + 4 * prime);
         if (store) {
 #pragma unroll
-            for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = red(shoup(x[0][e], w, ws, p), p);
+            for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = x[0][e];
         }
     }
 }
@@ -1082,9 +1083,10 @@ void fill_kernel_set(KernelSet& ks) {
     if constexpr (SPECIALISE && (SPEC_MASK & 64u))
         fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
     if constexpr (LOGE >= 6) {  // one transform per block (k_ntt1), coalesced row side at N = 4096
+        // register budgets measured best at N = 4096: 128 (forward), 96 (inverse)
         constexpr bool COAL = LOGN == 12 && LOGE == 6;
-        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false, 0, COAL>;
-        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true, 0, COAL>;
+        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false, 8, COAL>;
+        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true, 10, COAL>;
         ks.ntt_jobs_per_block = 1;
     } else {
         ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;

@@ -168,9 +168,13 @@ __device__ __forceinline__ void fwd_pass(uint32_t (&x)[NOPS][PL::E], const uint2
     }
 }
 
+// scale (inverse, pass 0, optional): {N^-1, Shoup, N^-1 w1, Shoup} with w1 the
+// twiddle of the last stage; that stage then writes (X + Y) N^-1 and
+// (X - Y) w1 N^-1 in [0, p), so no separate scaling pass is needed.
 template <class PL, int PASS, int NOPS>
 __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
-                                         int tau, int tm = 1, const uint2* __restrict__ twr = nullptr) {
+                                         int tau, int tm = 1, const uint2* __restrict__ twr = nullptr,
+                                         const uint32_t* __restrict__ scale = nullptr) {
     constexpr int R = PL::R(PASS), S0 = PL::S0(PASS), LOGD = PL::LOGD(PASS);
     constexpr int GS = 1 << R;
     constexpr int NV = PL::E >> R;
@@ -185,6 +189,24 @@ __device__ __forceinline__ void inv_pass(uint32_t (&x)[NOPS][PL::E], const uint2
             const uint2* twl = ROWS ? twr + PL::G * ((1 << l) - 1) + (l == 0 ? tau : 2 * tau)
                                     : tw + (tm << (S0 + l)) + (g << l);  // 16-byte aligned for l >= 1
             uint2 W = make_uint2(0u, 0u);
+            if (PASS == 0 && l == 0 && scale != nullptr) {  // last stage, N^-1 folded in (S0 = 0, g = 0)
+                const uint32_t n0 = __ldg(scale), n0s = __ldg(scale + 1), n1 = __ldg(scale + 2),
+                               n1s = __ldg(scale + 3);
+#pragma unroll
+                for (int b = 0; b < GS / 2; b++) {
+                    const int u = b;  // l = 0: half = 2^(R-1), one twiddle group
+#pragma unroll
+                    for (int o = 0; o < NOPS; o++) {
+                        uint32_t& X = x[o][v * GS + u];
+                        uint32_t& Y = x[o][v * GS + u + half];
+                        const uint32_t s = shoup_m(X + Y, n0, n0s, m);         // [0, 2p)
+                        const uint32_t d = shoup_m(X - Y + m.p2, n1, n1s, m);  // [0, 2p)
+                        X = __viaddmin_u32(s, m.np, s);
+                        Y = __viaddmin_u32(d, m.np, d);
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int b = 0; b < GS / 2; b++) {  // as in fwd_pass
                 const int h = b >> (R - 1 - l), j = b & (half - 1);
@@ -258,13 +280,14 @@ template <class PL, int PASS, int NOPS, class Sync = CtaSync>
 struct InvFrom {
     __device__ __forceinline__ static int run(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw,
                                               const Mod& m, int tau, uint32_t* sm, int stride, int buf,
-                                              Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr) {
+                                              Sync bar = Sync(), int tm = 1, const uint2* __restrict__ twr = nullptr,
+                                              const uint32_t* __restrict__ scale = nullptr) {
         if constexpr (PASS < 0) {
             return buf;
         } else {
             exchange<PL, PASS + 1, PASS, NOPS, Sync>(x, sm + (buf & 1) * stride, tau, stride == 0, bar);
-            inv_pass<PL, PASS, NOPS>(x, tw, m, tau, tm, twr);
-            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf + 1, bar, tm, twr);
+            inv_pass<PL, PASS, NOPS>(x, tw, m, tau, tm, twr, scale);
+            return InvFrom<PL, PASS - 1, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf + 1, bar, tm, twr, scale);
         }
     }
 };
@@ -283,9 +306,10 @@ __device__ __forceinline__ int ntt_forward(uint32_t (&x)[NOPS][PL::E], const uin
 template <class PL, int NOPS, class Sync = CtaSync>
 __device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uint2* __restrict__ tw, const Mod& m,
                                            int tau, uint32_t* sm, int stride, int buf, Sync bar = Sync(),
-                                           int tm = 1, const uint2* __restrict__ twr = nullptr) {
-    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, m, tau, tm, twr);
-    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf, bar, tm, twr);
+                                           int tm = 1, const uint2* __restrict__ twr = nullptr,
+                                           const uint32_t* __restrict__ scale = nullptr) {
+    inv_pass<PL, PL::NPASS - 1, NOPS>(x, tw, m, tau, tm, twr, scale);
+    return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf, bar, tm, twr, scale);
 }
 
 }  // namespace cy

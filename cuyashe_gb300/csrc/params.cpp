@@ -273,12 +273,19 @@ cy_status build_basis(Basis& b, int device, int n, const BigUInt& q, int mode, c
             b.h.ipsi_r[i] = tab->d_ipsi_r + (size_t)i * ROWS_WORDS;
         }
     }
-    std::vector<uint32_t> ninv(2 * (size_t)b.h.k);
+    // per prime: N^-1, and N^-1 times the twiddle of the last inverse stage
+    // (psi^-bitrev(1) = psi^-(NMAX/2)), each with its Shoup companion
+    std::vector<uint32_t> ninv(4 * (size_t)b.h.k);
     for (int i = 0; i < b.h.k; i++) {
         const uint32_t p = b.h.p[i];
         const uint32_t v = invmod32((uint32_t)(n % p), p);
-        ninv[2 * i] = v;
-        ninv[2 * i + 1] = shoup_of(v, p);
+        const uint32_t psi = find_psi(p);
+        const uint32_t w1 = powmod32(psi, 2ull * NMAX - NMAX / 2, p);
+        const uint32_t vw = mulmod32(v, w1, p);
+        ninv[4 * i] = v;
+        ninv[4 * i + 1] = shoup_of(v, p);
+        ninv[4 * i + 2] = vw;
+        ninv[4 * i + 3] = shoup_of(vw, p);
     }
     b.epi = epi_special(b.h.l32, b.h.k, b.h.mode);
     if (b.epi) {
