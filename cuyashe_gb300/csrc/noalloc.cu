@@ -1,9 +1,8 @@
 // noalloc.cu -- the polynomial product without any device allocation.
 //
-// Who needs it: callers that are not allowed to call cudaMalloc. A stream that
-// is being captured into a CUDA graph rejects cudaMalloc; a latency-critical
-// or serving path cannot afford cudaMalloc's implicit device-wide
-// synchronisation, which stalls every other stream; and a host whose device
+// Who needs it: callers that are not allowed to call cudaMalloc. A
+// latency-critical or serving path cannot afford cudaMalloc's implicit
+// device-wide synchronisation, which stalls every other stream; and a host whose device
 // memory belongs to another allocator (a framework's caching allocator, or a
 // process that admits work against a fixed memory budget) must not have a
 // library grab memory behind that allocator's back. cy_polymul grows a
@@ -77,12 +76,13 @@ extern "C" cy_status cy_polymul_noalloc(cy_ring* r, const uint64_t* d_a, const u
     const Basis& B = r->mul;
     const int n = B.h.n, k = B.h.k;
     const size_t per_product = (size_t)k * n * sizeof(uint32_t);
-    const size_t max_batch = CY_NOALLOC_SCRATCH_BYTES / per_product;
+    size_t max_batch = CY_NOALLOC_SCRATCH_BYTES / per_product;
+    if (max_batch > 65535) max_batch = 65535;  // one launch: the grid's y dimension holds the products
     if ((size_t)batch > max_batch) {
         char msg[200];
         std::snprintf(msg, sizeof(msg),
-                      "cy_polymul_noalloc: batch %d exceeds the static scratch; at most %zu products of this ring "
-                      "(N=%d, %d CRT primes) per call",
+                      "cy_polymul_noalloc: batch %d exceeds the limit of one call (static scratch and one launch); "
+                      "at most %zu products of this ring (N=%d, %d CRT primes) per call",
                       batch, max_batch, n, k);
         return set_error(CY_ERR_INVALID_ARGUMENT, msg);
     }
@@ -95,8 +95,9 @@ extern "C" cy_status cy_polymul_noalloc(cy_ring* r, const uint64_t* d_a, const u
     const BasisDev* Bd = B.d;
     long long stride = (long long)n * r->l64;
     void* args[] = {(void*)&Bd, (void*)&d_a, (void*)&stride, (void*)&d_b, (void*)&stride, (void*)&scratch};
-    CY_TRY(launch_noalloc(ks.mul_for(B.h.l64, false), "mul_noalloc", B.h.logn, dim3(k, batch), dim3(ks.threads),
-                          ks.smem_mul, st, args));
+    // blocks_per_prime > 1 for schedules that run one product on a pair of blocks
+    CY_TRY(launch_noalloc(ks.mul_for(B.h.l64, false), "mul_noalloc", B.h.logn, dim3(k * ks.blocks_per_prime, batch),
+                          dim3(ks.threads), ks.smem_mul, st, args));
     void* epi = epi_kernel(B.h.l32, EPI_MODQ);
     unsigned long long fl = 0;  // mod-q epilogue: no rounding estimate
     void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch, (void*)&fl};
