@@ -73,6 +73,11 @@ class ServeRequest(ctypes.Structure):
                 ("h_c2", ctypes.c_void_p), ("h_out", ctypes.c_void_p)]
 
 
+class ServeRequestDev(ctypes.Structure):
+    _fields_ = [("class_id", ctypes.c_int), ("relin", ctypes.c_int), ("d_c1", ctypes.c_void_p),
+                ("d_c2", ctypes.c_void_p), ("d_out", ctypes.c_void_p)]
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("batches", ctypes.c_uint64), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
@@ -148,6 +153,7 @@ SIGNATURES = {
     "cy_server_destroy": ([_vp], _i),
     "cy_server_register": ([_vp, _vp, ctypes.POINTER(_i)], _i),
     "cy_server_submit": ([_vp, ctypes.POINTER(ServeRequest), ctypes.POINTER(ctypes.c_uint64)], _i),
+    "cy_server_submit_device": ([_vp, ctypes.POINTER(ServeRequestDev), _i, ctypes.POINTER(ctypes.c_uint64)], _i),
     "cy_server_poll": ([_vp, ctypes.c_uint64, ctypes.POINTER(_i)], _i),
     "cy_server_wait": ([_vp, ctypes.c_uint64, _i], _i),
     "cy_server_drain": ([_vp, _i], _i),

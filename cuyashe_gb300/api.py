@@ -19,7 +19,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from . import (CY_OK, BLOB_KEYS, BlobInfo, PolymulJob, RingInfo, ServeRequest, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
+from . import (CY_OK, BLOB_KEYS, BlobInfo, PolymulJob, RingInfo, ServeRequest, ServeRequestDev, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
                _stream_handle, check, lib, limbs_of)
 
 
@@ -449,6 +449,34 @@ class Server:
                            h_c2=c2.ctypes.data if c2 is not None else 0, h_out=out.ctypes.data if out is not None else 0)
         t = ctypes.c_uint64(0)
         return lib().cy_server_submit(self.h, ctypes.byref(req), ctypes.byref(t))
+
+    def submit_device(self, class_id, c1, c2, out, relin=True) -> list:
+        """Queues requests on device-resident ciphertexts (``cy_server_submit_device``).
+
+        c1, c2, out: int64 CUDA tensors [count][N][L] (one request per row) or
+        sequences of device addresses; ``relin`` and ``class_id`` apply to every
+        request, or are per-request sequences. Returns the tickets."""
+        def addrs(x):
+            if hasattr(x, "data_ptr"):
+                step = x[0].numel() * x.element_size() if x.dim() == 3 else 0
+                return [x.data_ptr() + i * step for i in range(x.shape[0] if x.dim() == 3 else 1)]
+            return [int(a) for a in x]
+        a1, a2, ao = addrs(c1), addrs(c2), addrs(out)
+        n = len(a1)
+        cls = class_id if hasattr(class_id, "__len__") else [class_id] * n
+        rl = relin if hasattr(relin, "__len__") else [relin] * n
+        reqs = (ServeRequestDev * n)()
+        for i in range(n):
+            reqs[i].class_id = int(cls[i])
+            reqs[i].relin = 1 if rl[i] else 0
+            reqs[i].d_c1, reqs[i].d_c2, reqs[i].d_out = a1[i], a2[i], ao[i]
+        t = (ctypes.c_uint64 * n)()
+        check(lib().cy_server_submit_device(self.h, reqs, n, t), "cy_server_submit_device")
+        return list(t)
+
+    def submit_device_raw(self, reqs, n: int, tickets) -> int:
+        """``cy_server_submit_device`` on prepared ctypes arrays (no conversion)."""
+        return lib().cy_server_submit_device(self.h, reqs, n, tickets)
 
     def poll(self, ticket: int) -> bool:
         d = ctypes.c_int(0)

@@ -2,6 +2,7 @@
 #include <mutex>
 #include <vector>
 
+#include "host.h"
 #include "kernels.cuh"
 
 namespace cy {
@@ -210,6 +211,42 @@ void* addsub_kernel(int l64, bool sub) {
                                 {(void*)k_addsub<6, false>, (void*)k_addsub<6, true>}};
     if (l64 < 1 || l64 > 6) return nullptr;
     return table[l64][sub ? 1 : 0];
+}
+
+// Polynomials of `words` uint64 words between a list of device pointers and one
+// contiguous array (16-byte moves): gather ptrs[i] -> flat + i*words, or scatter
+// flat + i*words -> ptrs[i]. The serving loop's device-resident requests.
+template <bool GATHER>
+__global__ void k_poly_move(uint64_t* const* __restrict__ ptrs, uint64_t* __restrict__ flat, long long count,
+                            long long words) {
+    const long long half = words / 2;  // 16-byte units per polynomial (words is even: N >= 2)
+    const long long total = count * half;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long i = idx / half, w = idx - i * half;
+        uint4* f = reinterpret_cast<uint4*>(flat + i * words) + w;
+        uint4* q = reinterpret_cast<uint4*>(ptrs[i]) + w;
+        if (GATHER) *f = __ldg(q);
+        else *q = *f;
+    }
+}
+
+int trace_begin(const char* name, int logn, cudaStream_t st);
+void trace_end(int idx, cudaStream_t st);
+
+cy_status move_polys(uint64_t* const* d_ptrs, uint64_t* flat, int count, size_t words, bool gather,
+                     cudaStream_t st) {
+    if (count <= 0) return CY_OK;
+    const long long total = (long long)count * (long long)(words / 2);
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    long long cnt = count, w = (long long)words;
+    void* args[] = {(void*)&d_ptrs, (void*)&flat, (void*)&cnt, (void*)&w};
+    const int tr = trace_begin(gather ? "serve_gather" : "serve_scatter", 0, st);
+    const cudaError_t e = cudaLaunchKernel(gather ? (void*)k_poly_move<true> : (void*)k_poly_move<false>,
+                                           dim3((unsigned)blocks), dim3(256), args, 0, st);
+    trace_end(tr, st);
+    return e == cudaSuccess ? CY_OK : cuda_error(e, "serving gather/scatter");
 }
 
 void* crt_kernel() { return (void*)k_crt; }

@@ -14,6 +14,9 @@
 //     workspace, one device-to-host copy, an event;
 //   * retires batches whose event has completed, copies the results to the
 //     callers' buffers, records latencies and frees the budget.
+// Requests on device-resident ciphertexts (cy_server_submit_device) form their
+// own batches: their inputs are gathered on the device into the slot's buffers
+// and their products scattered to the callers' device buffers, with no host copy.
 // Batches of different contexts and sizes run concurrently on different
 // streams while new requests keep arriving. Evaluation keys stay resident in
 // each cy_yashe. Waits are host-side and bounded (cy_server_wait takes a
@@ -28,6 +31,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -40,10 +44,14 @@ static double now_us() {
     return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+cy_status move_polys(uint64_t* const* d_ptrs, uint64_t* flat, int count, size_t words, bool gather,
+                     cudaStream_t st);
+
 struct Request {
     int cls = 0;
     int relin = 1;
-    const uint64_t* h_c1 = nullptr;
+    bool dev = false;                // buffers are device memory (cy_server_submit_device)
+    const uint64_t* h_c1 = nullptr;  // host or device pointers, as `dev` says
     const uint64_t* h_c2 = nullptr;
     uint64_t* h_out = nullptr;
     double t_submit = 0;
@@ -130,7 +138,13 @@ struct Slot {
     size_t bytes = 0;
     size_t cap_words = 0;  // uint64 words of one output buffer (inputs hold twice as many)
     uint64_t *d_in = nullptr, *d_out = nullptr, *h_in = nullptr, *h_out = nullptr;
+    bool dev = false;            // the batch in flight is of device-resident requests
+    size_t cap_ptrs = 0;         // pointer lists of device-resident batches
+    uint64_t** h_ptrs = nullptr;  // page-locked: c1 of each request, then c2, then out
+    uint64_t** d_ptrs = nullptr;
     ~Slot() {
+        if (h_ptrs) cudaFreeHost(h_ptrs);
+        if (d_ptrs) cudaFree(d_ptrs);
         if (d_in) cudaFree(d_in);
         if (d_out) cudaFree(d_out);
         if (h_in) cudaFreeHost(h_in);
@@ -198,6 +212,19 @@ static cy_status grow_slot(Slot& s, size_t polys, size_t poly_words) {
     return CY_OK;
 }
 
+static cy_status grow_ptrs(Slot& s, size_t n) {
+    if (n <= s.cap_ptrs) return CY_OK;
+    const size_t want = std::max(2 * n, 2 * s.cap_ptrs);
+    if (s.h_ptrs) cudaFreeHost(s.h_ptrs);
+    if (s.d_ptrs) cudaFree(s.d_ptrs);
+    s.h_ptrs = s.d_ptrs = nullptr;
+    s.cap_ptrs = 0;
+    CY_CUDA(cudaMallocHost(&s.h_ptrs, want * sizeof(uint64_t*)));
+    CY_CUDA(cudaMalloc(&s.d_ptrs, want * sizeof(uint64_t*)));
+    s.cap_ptrs = want;
+    return CY_OK;
+}
+
 // One pass of the dispatcher. Bookkeeping happens under the lock; copies into
 // and out of the callers' buffers and the launches happen without it, so that
 // submitters are never held up by a batch being prepared. Only this thread
@@ -226,7 +253,8 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         const cy_yashe* y = S->classes[s.cls];
         d.poly = (size_t)y->ring->n * y->ring->l64;
         if (s.ids.size() * d.poly > s.cap_words) d.st = set_error(CY_ERR_INTERNAL, "serving slot too small");
-        for (uint64_t id : s.ids) d.outs.push_back(S->reqs[id].h_out);
+        if (!s.dev)  // device-resident results are already in the callers' buffers
+            for (uint64_t id : s.ids) d.outs.push_back(S->reqs[id].h_out);
         done.push_back(std::move(d));
     }
     if (!done.empty()) {
@@ -262,6 +290,7 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         if (s.busy || S->pending.empty()) continue;
         const int cls = S->reqs[S->pending.front()].cls;
         const int relin = S->reqs[S->pending.front()].relin;
+        const bool dev = S->reqs[S->pending.front()].dev;
         cy_yashe* y = S->classes[cls];
         const size_t per = request_bytes(y);
         int cap = S->cfg.max_batch;  // requests of this batch
@@ -269,10 +298,11 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
             cap = std::max(1, std::min(cap, (int)(S->cfg.batch_budget_us / S->us_per_req[cls])));
         std::vector<uint64_t> take;
         std::vector<const uint64_t*> in1, in2;
+        std::vector<uint64_t*> outs;
         size_t bytes = 0;
         for (auto it = S->pending.begin(); it != S->pending.end() && (int)take.size() < cap;) {
             const Request& r = S->reqs[*it];
-            if (r.cls != cls || r.relin != relin) {
+            if (r.cls != cls || r.relin != relin || r.dev != dev) {
                 ++it;
                 continue;
             }
@@ -280,11 +310,13 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
             take.push_back(*it);
             in1.push_back(r.h_c1);
             in2.push_back(r.h_c2);
+            outs.push_back(r.h_out);
             bytes += per;
             it = S->pending.erase(it);
         }
         if (take.empty()) break;  // the budget is full until a batch retires
         s.busy = true;  // reserved: not retired before its event is recorded below
+        s.dev = dev;
         s.cls = cls;
         s.ids = take;
         s.bytes = bytes;
@@ -296,7 +328,28 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         const size_t poly = (size_t)y->ring->n * y->ring->l64;
         cy_status st = grow_slot(s, nb, poly);
         if (st == CY_OK && (size_t)nb * poly > s.cap_words) st = set_error(CY_ERR_INTERNAL, "serving slot too small");
-        if (st == CY_OK) {
+        if (st == CY_OK && dev) {
+            // device-resident: pointer lists in, gather, multiply, scatter
+            st = grow_ptrs(s, 3 * (size_t)nb);
+            if (st == CY_OK) {
+                for (int i = 0; i < nb; i++) {
+                    s.h_ptrs[i] = const_cast<uint64_t*>(in1[i]);
+                    s.h_ptrs[nb + i] = const_cast<uint64_t*>(in2[i]);
+                    s.h_ptrs[2 * nb + i] = outs[i];
+                }
+                cudaError_t e = cudaEventRecord(s.ev_start, s.st);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(s.d_ptrs, s.h_ptrs, 3 * nb * sizeof(uint64_t*), cudaMemcpyHostToDevice, s.st);
+                if (e != cudaSuccess) st = cuda_error(e, "serving pointer lists");
+            }
+            if (st == CY_OK) st = move_polys(s.d_ptrs, s.d_in, 2 * nb, poly, true, s.st);
+            if (st == CY_OK) st = cy_yashe_mul_ws(y, &s.ws, s.d_in, s.d_in + nb * poly, s.d_out, nb, relin, s.st);
+            if (st == CY_OK) st = move_polys(s.d_ptrs + 2 * nb, s.d_out, nb, poly, false, s.st);
+            if (st == CY_OK) {
+                const cudaError_t e = cudaEventRecord(s.ev, s.st);
+                if (e != cudaSuccess) st = cuda_error(e, "serving event");
+            }
+        } else if (st == CY_OK) {
             std::vector<CopyTask> tasks;
             tasks.reserve(2 * nb);
             for (int i = 0; i < nb; i++) {
@@ -428,6 +481,43 @@ cy_status cy_server_submit(cy_server* S, const cy_serve_request* req, uint64_t* 
     S->reqs[id] = r;
     S->pending.push_back(id);
     *ticket = id;
+    S->cv_work.notify_one();
+    return CY_OK;
+}
+
+cy_status cy_server_submit_device(cy_server* S, const cy_serve_request_dev* reqs, int n, uint64_t* tickets) {
+    if (!S || (n > 0 && (!reqs || !tickets)) || n < 0) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(S->mu);
+    const double t = now_us();
+    for (int i = 0; i < n; i++) {
+        const cy_serve_request_dev& q = reqs[i];
+        if (q.class_id < 0 || q.class_id >= (int)S->classes.size() || !q.d_c1 || !q.d_c2 || !q.d_out ||
+            (((uintptr_t)q.d_c1 | (uintptr_t)q.d_c2 | (uintptr_t)q.d_out) & 15)) {
+            S->rejected++;
+            return set_error(CY_ERR_INVALID_ARGUMENT,
+                             "device request with an unknown class, NULL or unaligned buffers (index " +
+                                 std::to_string(i) + ")");
+        }
+        const size_t bytes = request_bytes(S->classes[q.class_id]);
+        if (bytes > S->cfg.device_budget_bytes) {
+            S->rejected++;
+            return set_error(CY_ERR_OUT_OF_MEMORY, "one request needs more device memory than the whole budget");
+        }
+        Request r;
+        r.cls = q.class_id;
+        r.relin = q.relin ? 1 : 0;
+        r.dev = true;
+        r.h_c1 = q.d_c1;
+        r.h_c2 = q.d_c2;
+        r.h_out = q.d_out;
+        r.t_submit = t;
+        r.bytes = bytes;
+        if (S->t_first == 0) S->t_first = t;
+        const uint64_t id = S->next_id++;
+        S->reqs[id] = r;
+        S->pending.push_back(id);
+        tickets[i] = id;
+    }
     S->cv_work.notify_one();
     return CY_OK;
 }

@@ -124,16 +124,16 @@ cy_status cy_poly_scalar_mul(cy_ring *ring, const uint64_t *d_a, const uint64_t 
                              int batch, cy_stream_t stream);
 
 /* The product c = a*b mod (x^N+1, q), like cy_polymul, for callers that must
- * not allocate device memory: code that records work into a CUDA graph
- * (cudaMalloc is refused while a stream is being captured), latency-critical
- * or serving paths that cannot take cudaMalloc's device-wide synchronisation,
- * and hosts whose device memory is owned by another allocator or a fixed
- * budget. It calls no cudaMalloc, cudaFree or allocating library routine: its
- * scratch is a fixed array of CY_NOALLOC_SCRATCH_BYTES in the library's device
- * image, held by every GPU that loads the library until the process exits.
+ * not allocate device memory: latency-critical or serving paths that cannot
+ * take cudaMalloc's device-wide synchronisation, and hosts whose device memory
+ * is owned by another allocator or admitted against a fixed budget. It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch is a fixed
+ * array of CY_NOALLOC_SCRATCH_BYTES in the library's device image, held by
+ * every GPU that loads the library until the process exits.
  * Limit: batch * (CRT primes) * N * 4 bytes must fit in that array (at N = 4096
- * and a 127-bit q, 113 products per call); larger batches are rejected with
- * CY_ERR_INVALID_ARGUMENT and a message giving the maximum. The first call on
+ * and a 127-bit q, 113 products per call), and batch <= 65535 (one launch);
+ * larger batches are rejected with CY_ERR_INVALID_ARGUMENT and a message
+ * giving the maximum. The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress); make
  * that first call before any stream capture. All calls share the array, so
  * calls that can overlap on the GPU race and must be serialised by the caller.
@@ -391,6 +391,25 @@ cy_status cy_server_register(cy_server *server, cy_yashe *y, int *class_id);
 /* Queues a request. Invalid requests (unknown class, NULL buffers) and requests
  * larger than the whole budget are rejected here and counted. */
 cy_status cy_server_submit(cy_server *server, const cy_serve_request *req, uint64_t *ticket);
+/* Requests on ciphertexts resident in device memory: the caller uploads them
+ * once (or keeps the results of earlier requests) and names them by device
+ * pointer. A batch of such requests is gathered on the device into the slot's
+ * buffers, multiplied, and each product written to its d_out, with no host copy
+ * in either direction; d_out stays on the device for the caller's next
+ * operation. Buffers are 16-byte aligned device memory of the server's device,
+ * [N][L] limbs of the class's ring; keep them alive and unchanged until the
+ * request completes. `n` requests are queued in one call (tickets[i] for
+ * reqs[i]); a rejected request stops the call at that index with its error, the
+ * ones before it stay queued. Device requests batch apart from host-buffer ones.
+ * The reference keeps each Polynomial's device copy between operations
+ * (src/polynomial.cpp:265-340) but has no request loop. */
+typedef struct cy_serve_request_dev {
+    int class_id;                /* from cy_server_register */
+    int relin;                   /* relinearise the product */
+    const uint64_t *d_c1, *d_c2; /* [N][L] ciphertexts in device memory */
+    uint64_t *d_out;             /* [N][L] result in device memory */
+} cy_serve_request_dev;
+cy_status cy_server_submit_device(cy_server *server, const cy_serve_request_dev *reqs, int n, uint64_t *tickets);
 cy_status cy_server_poll(cy_server *server, uint64_t ticket, int *done);
 /* Waits up to timeout_ms; returns the request's status (and forgets the ticket)
  * or CY_ERR_TIMEOUT (the request stays queued or running). */

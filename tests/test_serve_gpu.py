@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 Q62 = ring.largest_prime_below(2**62, 2**16)
 Q127 = ring.largest_prime_below(2**127, 2**16)
 Q190 = ring.largest_prime_below(2**190, 2**16)
+Q380 = ring.largest_prime_below(2**380, 2**16)
 
 
 @pytest.fixture(scope="module")
@@ -25,7 +26,9 @@ def setup():
 
     assert torch.cuda.is_available()
     ctxs = []
-    for n, q, t in [(1024, Q62, 257), (2048, Q127, 1024), (4096, Q127, 1024), (1024, Q190, 65537)]:
+    # the last two are the serving mix's 8192/190-bit and 16384/380-bit classes
+    for n, q, t in [(1024, Q62, 257), (2048, Q127, 1024), (4096, Q127, 1024), (1024, Q190, 65537),
+                    (8192, Q190, 65537), (16384, Q380, 65537)]:
         y = Yashe(n, q, t)
         y.keygen(n + t)
         ctxs.append(y)
@@ -47,7 +50,7 @@ def test_results_same_alone_and_in_the_mix(setup):
     cls = [srv.register(y) for y in ctxs]
     rng = np.random.default_rng(7)
     reqs = []
-    for i in range(160):
+    for i in range(192):
         c = int(rng.integers(0, len(ctxs)))
         y = ctxs[c]
         c1, c2 = _uniform(rng, y.n, y.q, y.L), _uniform(rng, y.n, y.q, y.L)
@@ -181,3 +184,96 @@ def test_time_budget_splits_batches(setup):
     assert np.array_equal(alone[0].cpu().numpy().view(np.uint64), outs[1][0][0])
     with pytest.raises(cy.CyError):
         Server(budget_bytes=2 << 30, streams=1, max_batch=4, batch_budget_us=-1)
+
+
+def test_device_resident_requests_same_alone_and_in_the_mix(setup):
+    """Requests naming ciphertexts already in device memory (uploaded once,
+    results left on the device) are gathered, multiplied and scattered on the
+    GPU: every result equals the same multiply alone, for every class of the
+    serving mix, while host-buffer requests of the same classes run beside them."""
+    import torch
+
+    cy, Server, ctxs = setup
+    srv = Server(budget_bytes=4 << 30, streams=4, max_batch=32)
+    cls = [srv.register(y) for y in ctxs]
+    rng = np.random.default_rng(21)
+    per = 12
+    dev = []
+    for k, y in enumerate(ctxs):
+        c1 = np.stack([_uniform(rng, y.n, y.q, y.L) for _ in range(per)])
+        c2 = np.stack([_uniform(rng, y.n, y.q, y.L) for _ in range(per)])
+        d1 = torch.from_numpy(c1.view(np.int64)).cuda()
+        d2 = torch.from_numpy(c2.view(np.int64)).cuda()
+        do = torch.zeros_like(d1)
+        dev.append((k, d1, d2, do))
+    torch.cuda.synchronize()
+    tickets = []
+    host = []
+    for k, d1, d2, do in dev:  # device requests of every class, relin on all but the first
+        relin = [j > 0 for j in range(per)]
+        tickets += srv.submit_device(cls[k], d1, d2, do, relin=relin)
+        y = ctxs[k]
+        a, b = _uniform(rng, y.n, y.q, y.L), _uniform(rng, y.n, y.q, y.L)
+        o = np.zeros_like(a)
+        host.append((k, a, b, o, srv.submit(cls[k], a, b, o)))
+    for t in tickets:
+        srv.wait(t)
+    for k, a, b, o, t in host:
+        srv.wait(t)
+    st = srv.stats()
+    assert st.failed == 0 and st.completed == len(tickets) + len(host)
+    for k, d1, d2, do in dev:
+        y = ctxs[k]
+        for j in range(per):
+            alone = y.mul(d1[j:j + 1], d2[j:j + 1], relin=j > 0)
+            torch.cuda.synchronize()
+            assert torch.equal(alone[0], do[j]), "class %d request %d" % (k, j)
+    for k, a, b, o, t in host:
+        alone = ctxs[k].mul(torch.from_numpy(a.view(np.int64))[None].cuda(),
+                            torch.from_numpy(b.view(np.int64))[None].cuda(), relin=True)
+        torch.cuda.synchronize()
+        assert np.array_equal(alone[0].cpu().numpy().view(np.uint64), o)
+    srv.close()
+
+
+def test_device_requests_refused_on_host(setup):
+    import torch
+
+    cy, Server, ctxs = setup
+    y = ctxs[0]
+    srv = Server(budget_bytes=1 << 30, streams=1, max_batch=4)
+    c = srv.register(y)
+    d = torch.zeros((2, y.n, y.L), dtype=torch.int64, device="cuda")
+    with pytest.raises(cy.CyError):
+        srv.submit_device(c + 7, d, d, d)                      # unknown class
+    with pytest.raises(cy.CyError):
+        srv.submit_device(c, [d.data_ptr() + 8], [d.data_ptr()], [d.data_ptr()])  # not 16-byte aligned
+    assert srv.stats().rejected == 2
+    srv.close()
+
+
+def test_wait_deadline_on_a_running_batch(setup):
+    """A wait whose deadline passes while its request is still queued or running
+    returns CY_ERR_TIMEOUT and leaves the request alone; a later wait succeeds."""
+    import torch
+
+    cy, Server, ctxs = setup
+    y = ctxs[5]  # N = 16384, 380-bit q: a large batch takes milliseconds on the GPU
+    srv = Server(budget_bytes=8 << 30, streams=1, max_batch=128)
+    c = srv.register(y)
+    rng = np.random.default_rng(5)
+    a = np.stack([_uniform(rng, y.n, y.q, y.L) for _ in range(2)])
+    d1 = torch.from_numpy(np.repeat(a[:1], 128, axis=0).view(np.int64)).cuda()
+    d2 = torch.from_numpy(np.repeat(a[1:], 128, axis=0).view(np.int64)).cuda()
+    do = torch.zeros_like(d1)
+    torch.cuda.synchronize()
+    tickets = srv.submit_device(c, d1, d2, do)
+    st = cy.lib().cy_server_wait(srv.h, tickets[-1], 0)  # the deadline has passed at once
+    assert st == -7, st
+    for t in tickets:
+        srv.wait(t, timeout_ms=120000)
+    assert srv.stats().completed == 128
+    alone = y.mul(d1[:1], d2[:1], relin=True)
+    torch.cuda.synchronize()
+    assert torch.equal(alone[0], do[127])
+    srv.close()
