@@ -210,7 +210,73 @@ def _q380():
     return p
 
 
-def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2024, batch_budget_us=0):
+SERVE_P99_BOUND_MS = 10.0  # latency bound of the capacity figure
+SERVE_SWEEP = (20000.0, 40000.0, 80000.0, 160000.0, 320000.0)  # offered rates of the capacity sweep
+
+
+def _poisson(rng, rate_per_s, count):
+    import numpy as np
+
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
+
+
+def _resident_run(srv, classes, ids, dev, rate_per_s, seconds, seed):
+    """Poisson arrivals of requests on device-resident ciphertexts, submitted in
+    arrival order (every request due by now in one cy_server_submit_device
+    call); returns the server's statistics of the run."""
+    import ctypes
+
+    import numpy as np
+
+    from cuyashe_gb300 import ServeRequestDev
+
+    rng = np.random.default_rng(seed)
+    count = int(rate_per_s * seconds)
+    arrivals = _poisson(rng, rate_per_s, count)
+    weights = np.array([c["w"] for c in classes])
+    kinds = rng.choice(len(classes), size=count, p=weights / weights.sum())
+    picks = rng.integers(0, 8, size=(count, 2))
+    # requests prepared up front as one array of cy_serve_request_dev records
+    rec = np.zeros(count, dtype=np.dtype([("cls", "<i4"), ("relin", "<i4"), ("c1", "<u8"), ("c2", "<u8"),
+                                          ("out", "<u8")]))
+    assert rec.dtype.itemsize == ctypes.sizeof(ServeRequestDev)
+    base_ct = np.array([dev[k][0].data_ptr() for k in range(len(classes))], np.uint64)
+    base_out = np.array([dev[k][1].data_ptr() for k in range(len(classes))], np.uint64)
+    poly_b = np.array([c["poly_bytes"] for c in classes], np.uint64)
+    slots = np.array([dev[k][1].shape[0] for k in range(len(classes))], np.uint64)
+    pool = np.array([c["pool"] for c in classes], np.uint64)
+    rec["cls"] = np.array(ids)[kinds]
+    rec["relin"] = 1
+    rec["c1"] = base_ct[kinds] + picks[:, 0].astype(np.uint64) * poly_b[kinds]
+    rec["c2"] = base_ct[kinds] + (pool[kinds] + picks[:, 1].astype(np.uint64)) * poly_b[kinds]
+    rec["out"] = base_out[kinds] + (np.arange(count, dtype=np.uint64) % slots[kinds]) * poly_b[kinds]
+    tickets = (ctypes.c_uint64 * count)()
+    rsz, tsz = rec.dtype.itemsize, ctypes.sizeof(ctypes.c_uint64)
+    rbase, tbase = rec.ctypes.data, ctypes.addressof(tickets)
+    srv.reset_stats()
+    i = 0
+    t0 = time.perf_counter()
+    while i < count:
+        j = int(np.searchsorted(arrivals, time.perf_counter() - t0, side="right"))
+        if j > i:
+            st = srv.submit_device_raw(ctypes.cast(rbase + i * rsz, ctypes.POINTER(ServeRequestDev)), j - i,
+                                       ctypes.cast(tbase + i * tsz, ctypes.POINTER(ctypes.c_uint64)))
+            if st != 0:
+                raise RuntimeError("cy_server_submit_device: %d" % st)
+            i = j
+    lag_ms = (time.perf_counter() - t0 - arrivals[-1]) * 1000.0  # submission lag at the end of the trace
+    srv.drain()
+    for t in tickets:
+        srv.wait(t)
+    st = srv.stats()
+    return {"requests": count, "offered_rate_per_s": rate_per_s, "throughput_per_s": st.throughput_per_s,
+            "p50_ms": st.p50_us / 1000.0, "p99_ms": st.p99_us / 1000.0, "mean_ms": st.mean_us / 1000.0,
+            "batches": int(st.batches), "mean_batch": count / max(1, int(st.batches)), "failed": int(st.failed),
+            "submit_lag_ms": round(lag_ms, 3)}
+
+
+def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2024, batch_budget_us=0,
+                  sweep=SERVE_SWEEP, sweep_seconds=1.0):
     import numpy as np
     import torch
 
@@ -225,10 +291,11 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
         rng = np.random.default_rng(n)
         m = rng.integers(0, t, size=(2 * pool, n), dtype=np.uint64)
         ct = y.encrypt_host(m, seed=n)
-        classes.append({"y": y, "w": w, "ct": ct, "m": m, "t": t, "pool": pool, "n": n, "qbits": q.bit_length()})
+        classes.append({"y": y, "w": w, "ct": ct, "m": m, "t": t, "pool": pool, "n": n, "qbits": q.bit_length(),
+                        "poly_bytes": ct[0].nbytes})
     rng = np.random.default_rng(seed)
     count = int(rate_per_s * seconds)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
+    arrivals = _poisson(rng, rate_per_s, count)
     weights = np.array([c["w"] for c in classes])
     kinds = rng.choice(len(classes), size=count, p=weights / weights.sum())
     picks = rng.integers(0, 8, size=(count, 2))
@@ -242,14 +309,15 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
             for k, c in enumerate(classes) for i in range(64)]
     for t in warm:
         srv.wait(t)
-    # one served product per class decrypts to m1 * m2 mod t (slot 0 holds
-    # ct[0] * ct[pool]; checked before the timed run reuses the slots)
+    # the first 8 served products of every class decrypt to m1 * m2 mod t (slot i
+    # holds ct[i] * ct[pool + 3i mod 8]; checked before the timed run reuses the slots)
     decrypt_ok = True
     for k, c in enumerate(classes):
-        got = c["y"].decrypt(torch.from_numpy(outs[k][0:1].view(np.int64)).cuda()).cpu().numpy().view(np.uint64)
+        got = c["y"].decrypt(torch.from_numpy(outs[k][0:8].view(np.int64)).cuda()).cpu().numpy().view(np.uint64)
         PT = Ring(c["n"], c["t"])
-        exp = PT.polymul(PT.upload([c["m"][0].tolist()]), PT.upload([c["m"][c["pool"]].tolist()]))
-        decrypt_ok = decrypt_ok and bool((got[0] == exp.cpu().numpy().view(np.uint64)[0, :, 0]).all())
+        exp = PT.polymul(PT.upload([c["m"][i].tolist() for i in range(8)]),
+                         PT.upload([c["m"][c["pool"] + (i * 3) % 8].tolist() for i in range(8)]))
+        decrypt_ok = decrypt_ok and bool((got == exp.cpu().numpy().view(np.uint64)[..., 0]).all())
     srv.reset_stats()
     tickets = []
     t0 = time.perf_counter()
@@ -266,21 +334,44 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     st = srv.stats()
     served = {"requests": count, "offered_rate_per_s": rate_per_s, "throughput_per_s": st.throughput_per_s,
               "p50_ms": st.p50_us / 1000.0, "p99_ms": st.p99_us / 1000.0, "mean_ms": st.mean_us / 1000.0,
-              "batches": int(st.batches), "failed": int(st.failed), "peak_device_gb": st.peak_device_bytes / 1e9,
-              "batch_budget_us": batch_budget_us, "decrypt_ok": decrypt_ok,
+              "batches": int(st.batches), "mean_batch": count / max(1, int(st.batches)), "failed": int(st.failed),
+              "peak_device_gb": st.peak_device_bytes / 1e9, "batch_budget_us": batch_budget_us,
+              "api": "cy_server_submit (host buffers, copied in and out per request)",
               "mix": {"%d/%d/t=%d" % (c["n"], c["qbits"], c["t"]): c["w"] for c in classes}}
+
+    # ciphertexts resident in HBM: uploaded once, results left on the device
+    dev = {}
+    for k, c in enumerate(classes):
+        dev[k] = (torch.from_numpy(c["ct"].view(np.int64)).cuda(),
+                  torch.zeros((2048,) + c["ct"].shape[1:], dtype=torch.int64, device="cuda"))
+    torch.cuda.synchronize()
+    _resident_run(srv, classes, ids, dev, 20000.0, 0.25, seed + 1)  # warm-up of the device path
+    resident = _resident_run(srv, classes, ids, dev, rate_per_s, seconds, seed + 2)
+    resident["api"] = "cy_server_submit_device (ciphertexts and results in device memory)"
+    # capacity: offered rates until the server no longer keeps up within the bound
+    points = []
+    capacity = 0.0
+    for r in sweep:
+        pt = _resident_run(srv, classes, ids, dev, r, sweep_seconds, seed + int(r))
+        points.append({k: pt[k] for k in ("offered_rate_per_s", "throughput_per_s", "p50_ms", "p99_ms",
+                                           "mean_batch", "submit_lag_ms")})
+        ok = pt["throughput_per_s"] >= 0.95 * r and pt["p99_ms"] <= SERVE_P99_BOUND_MS and pt["failed"] == 0
+        if ok:
+            capacity = r
+        else:
+            break
     srv.close()
+    del dev
 
     # the plain per-request path on the same trace prefix: one multiply per
     # request, in arrival order, host buffers copied in and out each time
     lat = []
-    stream = torch.cuda.current_stream()
-    dev = {}
+    devp = {}
     for k, c in enumerate(classes):
         shp = c["ct"].shape[1:]
-        dev[k] = (torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
-                  torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
-                  torch.empty((1,) + shp, dtype=torch.int64, device="cuda"))
+        devp[k] = (torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
+                   torch.empty((1,) + shp, dtype=torch.int64, device="cuda"),
+                   torch.empty((1,) + shp, dtype=torch.int64, device="cuda"))
     pinned = {k: torch.from_numpy(c["ct"].view(np.int64)).pin_memory() for k, c in enumerate(classes)}
     t0 = time.perf_counter()
     for i in range(min(plain_prefix, count)):
@@ -288,7 +379,7 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
             pass
         k = int(kinds[i])
         c = classes[k]
-        d1, d2, do = dev[k]
+        d1, d2, do = devp[k]
         d1[0].copy_(pinned[k][picks[i, 0]], non_blocking=True)
         d2[0].copy_(pinned[k][c["pool"] + picks[i, 1]], non_blocking=True)
         c["y"].mul(d1, d2, relin=True, out=do)
@@ -298,7 +389,13 @@ def serving_bench(cy, rate_per_s=20000.0, seconds=1.0, plain_prefix=2000, seed=2
     lat = np.array(lat) * 1000.0
     plain = {"requests": len(lat), "throughput_per_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
              "p99_ms": float(np.percentile(lat, 99))}
-    return {"continuous_batching": served, "plain_per_request": plain}
+    out = {"continuous_batching": served, "resident": resident,
+           "capacity": {"p99_bound_ms": SERVE_P99_BOUND_MS, "capacity_per_s": capacity, "sweep": points,
+                        "api": "cy_server_submit_device", "seconds_per_rate": sweep_seconds},
+           "plain_per_request": plain, "decrypt_ok": decrypt_ok, "decrypt_checked_per_class": 8}
+    if not decrypt_ok:  # a wrong product invalidates every serving figure
+        out = {"invalid": "decryption of served products failed", "decrypt_ok": False}
+    return out
 
 
 # ----------------------------------------------------------------------------
@@ -405,6 +502,52 @@ def time_steps(fn, steps: int, stream):
     return start.elapsed_time(end)
 
 
+def kernel_counts(tuning: str) -> dict:
+    """Warp instructions and DRAM bytes per job of the kernels of the headline
+    step, for the schedules in `tuning` (cy_tuning_export), from the committed ncu
+    summary profiles/kernel_counts_n4096.json; {} when it has no such entry."""
+    path = os.path.join(ROOT, "profiles", "kernel_counts_n4096.json")
+    if not os.path.exists(path):
+        return {}
+    per = json.load(open(path))["per_unit"]
+    tuned = dict(item.split("=") for item in tuning.split(";") if item.startswith("n4096.l2."))
+    out = {}
+    for name, op in (("mul_centered", "mulc"), ("keyswitch", "ks"), ("mul", "mul")):
+        key = "%s=%s" % (op, tuned.get("n4096.l2." + op, "0"))
+        if key in per:
+            out[name] = dict(per[key], source=key)
+    for name in ("epi_yashe", "epi_modq"):
+        if name in per:
+            out[name] = dict(per[name], source=name)
+    return out
+
+
+def int_roofline(kernels: dict, counts: dict, jobs: int, sm_mhz: float, sms: int, ms_per_step: float):
+    """Issue-slot roofline of the integer-bound kernels: executed warp
+    instructions (ncu, per job) x jobs / kernel time, against SMs x 4 schedulers
+    x the sampled SM clock. One row per kernel of the step and the whole step."""
+    if not counts or not sm_mhz:
+        return None
+    peak = sms * 4 * sm_mhz * 1e6  # warp instructions per second
+    rows = {}
+    step_inst = 0.0
+    for name, k in kernels.items():
+        c = counts.get(name.split("_n")[0])
+        if not c or k["ms"] <= 0:
+            continue
+        inst = c["warp_inst"] * jobs
+        step_inst += inst
+        rate = inst / (k["ms"] / 1000.0)
+        rows[name] = {"warp_inst_per_launch": inst / k["launches"], "achieved": rate, "frac": round(rate / peak, 4),
+                      "schedule": c["source"]}
+    top = max(kernels, key=lambda n: kernels[n]["ms"])
+    return {"bound": "issue", "unit": "warp instructions/s", "peak": peak,
+            "peak_basis": "%d SMs x 4 schedulers x %.0f MHz (median sampled SM clock)" % (sms, sm_mhz),
+            "kernel": top, "achieved": rows.get(top, {}).get("achieved"), "frac": rows.get(top, {}).get("frac"),
+            "kernels": rows, "step_frac": round(step_inst / (ms_per_step / 1000.0) / peak, 4),
+            "source": "profiles/kernel_counts_n4096.json (ncu smsp__inst_executed.sum per job)"}
+
+
 def kernel_bytes(name: str, launches: int, jobs: int, k_tensor: int, k_relin: int, ell: int):
     """Algorithmic bytes moved by all launches of one kernel over `jobs` jobs."""
     res = N * 4
@@ -439,7 +582,10 @@ def run_ours(args):
     if not args.no_autotune:
         Y.autotune(batch=512)
     tuning = cy.tuning_export()
-    C1, C2, m1, m2, idx1, idx2 = make_inputs(Y, B, pool=32, seed=77 + rank)
+    # weak scaling: each rank multiplies its own contiguous share (B pairs) of the
+    # job's world * B pairs; no data-path collective
+    p_start, p_stop = replicas.shard(world * B, rank, world)
+    C1, C2, m1, m2, idx1, idx2 = make_inputs(Y, p_stop - p_start, pool=32, seed=77 + p_start)
     OUT = Y.ring.empty(B)
     Y.mul(C1, C2, relin=True, out=OUT)
     dec = Y.decrypt(OUT[:4]).cpu().numpy().view(np.uint64)
@@ -499,16 +645,16 @@ def run_ours(args):
     peak, peak_kind = read_peaks()
     top_bytes = kernel_bytes(top, kernels[top]["launches"], B, info.tensor_primes, info.relin_primes, info.ell)
     top_gbs = top_bytes / (kernels[top]["ms"] / 1000.0) / 1e9
+    # measured counts per job of the schedule each kernel ran with (ncu, committed summary)
+    counts = kernel_counts(tuning)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_per_job.json")
-    if os.path.exists(tpath):
-        tj = json.load(open(tpath))
-        per_job = tj.get(top.split("_n")[0])
-        if per_job:
-            traffic = per_job * B / kernels[top]["launches"]
+    top_counts = counts.get(top.split("_n")[0])
+    if top_counts:
+        traffic = top_counts["dram_bytes"] * B / kernels[top]["launches"]
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(top_gbs, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(top_gbs / peak, 4), "peak_kind": peak_kind,
-                "traffic": traffic, "algorithmic_bytes_per_launch": top_bytes / kernels[top]["launches"]}
+                "traffic": traffic, "algorithmic_bytes_per_launch": top_bytes / kernels[top]["launches"],
+                "traffic_source": top_counts["source"] if top_counts else None}
     step_bytes = B * 3 * CT_BYTES + info.ell * N * L * 8
     step_gbs = step_bytes / (ms_max / args.steps / 1000.0) / 1e9
 
@@ -631,10 +777,11 @@ def run_ours(args):
     except Exception as e:
         log("ntt bench failed:", e)
 
-    # ---- mixed batch: 512 products, N over {1024..8192}, q of 62/127/190 bits ---
+    # ---- mixed batch: 512 products, N over {1024..8192}, q of 62/127/190 bits, ---
+    # ---- and a batch of HE multiplies of mixed N and CRT depth: one launch each ---
     mixed = None
     try:
-        from cuyashe_gb300.api import MixedBatch, polymul_batched, polymul_batched_status
+        from cuyashe_gb300.api import MixedPlan
 
         mq = {62: 4611686018427322369, 127: Q_YASHE,
               190: 1569275433846670190958947355801916604025588861116000698369}
@@ -658,12 +805,14 @@ def run_ours(args):
             Cm = Rm.empty(cnt)
             rings[(n_, b_)], bufs[(n_, b_)] = Rm, (Am, Bm, Cm)
             for j in range(cnt):
-                jobs.append((Rm, Am[j:j + 1], Bm[j:j + 1], Cm[j:j + 1]))
+                jobs.append(("mul", Rm, Am[j:j + 1], Bm[j:j + 1], Cm[j:j + 1]))
         order = list(range(len(jobs)))
         rngm.shuffle(order)
         jobs = [jobs[i] for i in order]
-        polymul_batched(jobs)
-        polymul_batched_status()
+        plan = MixedPlan(jobs)  # sized and uploaded once; launches allocate nothing
+        sched = plan.autotune()
+        plan.launch()
+        plan.status()
         ref = {key: bufs[key][2].clone() for key in bufs}
 
         def grouped():
@@ -675,14 +824,75 @@ def run_ours(args):
         torch.cuda.synchronize()
         same = all(torch.equal(ref[key], bufs[key][2]) for key in bufs)
         msteps = max(5, args.steps // 4)
-        mb = MixedBatch(jobs)  # the job array is built once, outside the timing
-        t_one = time_steps(lambda: mb.run(), msteps, stream)
+        t_one = time_steps(lambda: plan.launch(), msteps, stream)
+        plan.status()
+        g_mix = plan.graph()
+        t_graph = time_steps(lambda: g_mix.launch(stream), msteps, stream)
         t_grp = time_steps(grouped, msteps, stream)
-        polymul_batched_status()
-        mixed = {"products": len(jobs), "classes": len(groups),
+        mixed = {"products": len(jobs), "classes": len(groups), "schedule": sched,
                  "one_launch_products_per_s": len(jobs) * msteps / (t_one / 1000.0),
+                 "graph_products_per_s": len(jobs) * msteps / (t_graph / 1000.0),
                  "per_ring_products_per_s": len(jobs) * msteps / (t_grp / 1000.0),
                  "one_launch_matches_per_ring": bool(same)}
+        del plan, g_mix
+
+        # HE multiplies (relinearised) of four (N, q, t) classes in one launch
+        he_classes = [(2048, mq[62], 17), (4096, mq[127], 1024), (8192, mq[190], 65537), (1024, mq[190], 65537)]
+        he_jobs, he_groups, he_msgs = [], [], []
+        per_cls = 64
+        for k_, (n_, q_, t_) in enumerate(he_classes):
+            Yc = cy.Yashe(n_, q_, t_)
+            Yc.keygen(500 + k_)
+            pool = 4
+            hm = torch.from_numpy(rngm.integers(0, t_, size=(2 * pool, n_), dtype=np.int64)).cuda()
+            ct = Yc.encrypt(hm, seed=700 + k_)
+            hi1 = torch.arange(per_cls, device="cuda") % pool
+            hi2 = pool + (torch.arange(per_cls, device="cuda") * 3) % pool
+            C1c, C2c = ct[hi1].contiguous(), ct[hi2].contiguous()
+            Oc = Yc.ring.empty(per_cls)
+            he_groups.append((Yc, C1c, C2c, Oc))
+            he_msgs.append((hm, hi1, hi2))
+            for j in range(per_cls):
+                he_jobs.append(("yashe", Yc, C1c[j:j + 1], C2c[j:j + 1], Oc[j:j + 1], True))
+        order = list(range(len(he_jobs)))
+        rngm.shuffle(order)
+        he_jobs = [he_jobs[i] for i in order]
+        hplan = MixedPlan(he_jobs)
+        hsched = hplan.autotune()
+        hplan.launch()
+        hplan.status()
+        he_ref = [o.clone() for (_, _, _, o) in he_groups]
+
+        def he_grouped():
+            for Yc, C1c, C2c, Oc in he_groups:
+                Yc.mul(C1c, C2c, relin=True, out=Oc)
+
+        he_grouped()
+        torch.cuda.synchronize()
+        he_same = all(torch.equal(r_, g_[3]) for r_, g_ in zip(he_ref, he_groups))
+        # decryption of the one-launch results of every class
+        he_dec = True
+        for (Yc, _, _, _), (hm, hi1, hi2), r_ in zip(he_groups, he_msgs, he_ref):
+            got = Yc.decrypt(r_[:2]).cpu().numpy().view(np.uint64)
+            PT = cy.Ring(Yc.n, Yc.t)
+            exp = PT.polymul(PT.upload(hm[hi1[:2]].cpu().numpy().astype(object).tolist()),
+                             PT.upload(hm[hi2[:2]].cpu().numpy().astype(object).tolist()))
+            he_dec = he_dec and bool((got == exp.cpu().numpy().view(np.uint64)[..., 0]).all())
+        t_he = time_steps(lambda: hplan.launch(), msteps, stream)
+        hplan.status()
+        g_he = hplan.graph()
+        t_he_graph = time_steps(lambda: g_he.launch(stream), msteps, stream)
+        t_he_grp = time_steps(he_grouped, msteps, stream)
+        nhe = len(he_jobs)
+        mixed["he_multiplies"] = {
+            "jobs": nhe, "classes": ["%d/%d/t=%d" % (n_, q_.bit_length(), t_) for n_, q_, t_ in he_classes],
+            "schedule": hsched,
+            "one_launch_he_mults_per_s": nhe * msteps / (t_he / 1000.0),
+            "graph_he_mults_per_s": nhe * msteps / (t_he_graph / 1000.0),
+            "per_context_he_mults_per_s": nhe * msteps / (t_he_grp / 1000.0),
+            "one_launch_over_per_context": t_he_grp / t_he,
+            "one_launch_matches_per_context": bool(he_same), "decrypt_ok": bool(he_dec)}
+        del hplan, g_he
         log("mixed batch:", mixed)
     except Exception as e:  # reported, not fatal for the headline
         log("mixed batch failed:", e)
@@ -740,6 +950,13 @@ def run_ours(args):
     except Exception as e:  # the baseline must not sink the GPU number
         log("cpu baseline failed:", e)
 
+    clk = clocks.summary()
+    try:
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        int_roof = int_roofline(kernels, counts, B, clk.get("sm_mhz") or 0.0, sms, ms_max / args.steps)
+    except Exception as e:
+        log("integer roofline failed:", e)
+        int_roof = None
     line = {
         "metric": METRIC, "value": value, "unit": "HE mults/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -748,12 +965,13 @@ def run_ours(args):
                    "batch_pairs_per_gpu": B, "tensor_primes": info.tensor_primes, "relin_primes": info.relin_primes,
                    "l2": "inputs larger than L2 (%.0f MB per step)" % (2 * B * CT_BYTES / 1e6),
                    "parallelism": "replicas x%d" % world, "schedules": tuning},
-        "clocks": clocks.summary(),
+        "clocks": clk,
         "e2e": {"value": e2e_rate, "unit": "HE mults/s", "h2d_bytes_per_step": 2 * B * CT_BYTES,
                 "d2h_bytes_per_step": B * CT_BYTES, "output_matches_device": e2e_ok,
                 "api": "cy_yashe_mul_host (page-locked host buffers, host wall clock)", "copy_alone": copy_gbs},
         "gpu_launches": launches,
         "roofline": roofline,
+        "int_roofline": int_roof,
         "step_roofline": {"bound": "hbm", "achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
                           "frac": round(step_gbs / peak, 4), "algorithmic_bytes_per_step": step_bytes},
         "kernels": kernels,
@@ -775,6 +993,112 @@ def run_ours(args):
     replicas.close(rep)
 
 
+def ncu_schedules(batch: int = 256):
+    """One call of every N = 4096 schedule of the product (plain and centred),
+    the keyswitch and the standalone NTT (forced with cy_tuning_import) between
+    cudaProfilerStart/Stop, for ncu's per-schedule counts; prints the order."""
+    import numpy as np
+    import torch
+
+    import cuyashe_gb300 as cy
+
+    cy.lib()
+
+    def variants(op):
+        out = []
+        for v in range(64):
+            try:
+                cy.tuning_import("n%d.l2.%s=%d" % (N, op, v))
+            except cy.CyError:
+                break
+            out.append(v)
+        return out
+
+    Y = cy.Yashe(N, Q_YASHE, T, W_BITS, 8.0)
+    Y.keygen(1)
+    R = cy.Ring(N, Q_POLY)
+    rng = np.random.default_rng(5)
+    A = torch.from_numpy(rng.integers(0, 2**63, size=(batch, N, L), dtype=np.uint64).view(np.int64)).cuda()
+    A[..., 1] &= (1 << 62) - 1  # < 2^126 < q
+    Bt = A.flip(0).contiguous()
+    O = Y.ring.empty(batch)
+    RES = torch.zeros((batch, R.k, N), dtype=torch.int32, device="cuda")
+    plan = [(op, v) for op in ("mul", "mulc", "ks", "ntt") for v in variants(op)]
+
+    def run(op, v):
+        cy.tuning_import("n%d.l2.%s=%d" % (N, op, v))
+        if op == "mul":
+            R.polymul(A, Bt, out=O)
+        elif op == "mulc":
+            Y.mul(A, Bt, relin=False, out=O)
+        elif op == "ks":
+            Y.keyswitch(A, out=O)
+        else:
+            R.ntt(RES)
+            R.ntt(RES, inverse=True)
+
+    for op, v in plan:
+        run(op, v)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    for op, v in plan:
+        run(op, v)
+        torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print("ORDER", ";".join("%s=%d" % p for p in plan), flush=True)
+
+
+def _free_port() -> int:
+    import socket
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def launch_ranks(args, argv):
+    """`--gpus N` (N > 1) outside a launcher: start N ranks of this script with
+    torch.distributed.run on this node (one replica per GPU) and return their
+    exit status; None when this process already is a rank or N == 1."""
+    if args.gpus <= 1 or "WORLD_SIZE" in os.environ:
+        return None
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.abspath(__file__)] + argv
+    log("launching %d ranks:" % args.gpus, " ".join(cmd))
+    return subprocess.call(cmd)
+
+
+def cpu_dry_run(args):
+    """The replica bookkeeping of a run without CUDA (gloo): every rank takes its
+    contiguous share of the job's pairs, times a stand-in step, and rank 0 prints
+    one line with the world size and every rank's share. For tests of the
+    launcher; no GPU figure is measured."""
+    from cuyashe_gb300 import replicas
+
+    rep = replicas.from_env("gloo")
+    total = rep.world * args.batch
+    start, stop = replicas.shard(total, rep.rank, rep.world)
+    replicas.barrier(rep)
+    t0 = time.perf_counter()
+    acc = 0
+    for _ in range(args.steps):
+        acc += sum(range(start, stop))  # stand-in work on this rank's share
+    ms = (time.perf_counter() - t0) * 1000.0
+    ms_max = replicas.max_over_ranks(rep, ms)
+    units = replicas.sum_over_ranks(rep, stop - start)
+    if rep.is_root:
+        line = {"metric": METRIC, "value": None, "unit": "HE mults/s", "n_gpus": rep.world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / max(1, args.steps), "higher_is_better": True,
+                "scaling": "weak", "dry_run": True, "pairs_per_step": int(units),
+                "shards": [list(replicas.shard(total, r, rep.world)) for r in range(rep.world)],
+                "config": {"workload": "yashe_mul_relin N=4096 log2q=127 t=1024 w=2^32 ell=4",
+                           "batch_pairs_per_gpu": args.batch, "parallelism": "replicas x%d" % rep.world}}
+        print(json.dumps(line), flush=True)
+    replicas.close(rep)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -791,11 +1115,23 @@ def main():
                     help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
     ap.add_argument("--ncu-deep", type=int, default=0, metavar="PAIRS",
                     help="the same for one autotuned deep-level step (N=16384, 380-bit q) of PAIRS pairs")
+    ap.add_argument("--ncu-schedules", action="store_true",
+                    help="one call of every N=4096 schedule inside cudaProfilerStart/Stop, exit (for ncu)")
+    ap.add_argument("--cpu-dry-run", action="store_true",
+                    help="ranks and shares only, without CUDA (tests of the multi-GPU launcher)")
     args = ap.parse_args()
+    rc = launch_ranks(args, sys.argv[1:])
+    if rc is not None:
+        sys.exit(rc)
+    if args.cpu_dry_run:
+        cpu_dry_run(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         log("note: warm-up raised to 3")
         args.warmup = 3
-    if args.impl == "reference":
+    if args.ncu_schedules:
+        ncu_schedules()
+    elif args.impl == "reference":
         run_reference(args)
     elif args.serving_only > 0:
         import cuyashe_gb300 as cy

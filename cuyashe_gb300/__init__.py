@@ -99,6 +99,11 @@ class PolymulJob(ctypes.Structure):
                 ("d_c", ctypes.c_void_p)]
 
 
+class MixedJobC(ctypes.Structure):
+    _fields_ = [("ring", ctypes.c_void_p), ("yashe", ctypes.c_void_p), ("relin", ctypes.c_int),
+                ("d_a", ctypes.c_void_p), ("d_b", ctypes.c_void_p), ("d_c", ctypes.c_void_p)]
+
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -122,6 +127,15 @@ SIGNATURES = {
     "cy_polymul_batched": ([ctypes.POINTER(PolymulJob), _i, _vp], _i),
     "cy_polymul_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp], _i),
     "cy_polymul_batched_status": ([_vp], _i),
+    "cy_mixed_plan_create": ([ctypes.POINTER(MixedJobC), _i, ctypes.POINTER(_vp)], _i),
+    "cy_mixed_plan_destroy": ([_vp], _i),
+    "cy_mixed_plan_launch": ([_vp, _vp], _i),
+    "cy_mixed_plan_status": ([_vp, _vp], _i),
+    "cy_mixed_plan_set_schedule": ([_vp, _i], _i),
+    "cy_mixed_plan_get_schedule": ([_vp, ctypes.POINTER(_i)], _i),
+    "cy_mixed_plan_autotune": ([_vp, _vp], _i),
+    "cy_mixed_plan_test_starve": ([_vp, _i, ctypes.c_uint], _i),
+    "cy_mixed_plan_graph_create": ([_vp, ctypes.POINTER(_vp)], _i),
     "cy_ntt": ([_vp, _vp, _i, _i, _vp], _i),
     "cy_crt": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_icrt": ([_vp, _vp, _vp, _i, _vp], _i),
@@ -256,4 +270,4 @@ class Trace:
         return False
 
 
-from .api import Ring, Yashe, Workspace  # noqa: E402,F401
+from .api import MixedPlan, Ring, Yashe, Workspace  # noqa: E402,F401

@@ -19,7 +19,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from . import (CY_OK, BLOB_KEYS, BlobInfo, PolymulJob, RingInfo, ServeRequest, ServeRequestDev, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
+from . import (CY_OK, BLOB_KEYS, BlobInfo, MixedJobC, PolymulJob, RingInfo, ServeRequest, ServeRequestDev, ServerConfig, ServerStats, YasheInfo, YasheParams, _ptr,
                _stream_handle, check, lib, limbs_of)
 
 
@@ -251,6 +251,67 @@ class MixedBatch:
 
     def run(self, stream=None) -> None:
         check(lib().cy_polymul_batched(self.arr, len(self._jobs), _stream_handle(stream)), "cy_polymul_batched")
+
+
+class MixedPlan:
+    """A prepared mixed batch (``cy_mixed_plan_*``): polynomial products and YASHE
+    multiplies of rings of different N and q, launched as one persistent kernel.
+
+    jobs: ("mul", ring, a, b, c) or ("yashe", scheme, c1, c2, out, relin) with
+    device tensors [N][L]. Creation allocates and uploads; ``launch`` issues one
+    memset and one kernel, without allocation or host synchronisation."""
+
+    def __init__(self, jobs: Sequence[tuple]):
+        self._jobs = list(jobs)
+        arr = (MixedJobC * len(self._jobs))()
+        for i, j in enumerate(self._jobs):
+            if j[0] == "mul":
+                _, r, a, b, c = j
+                arr[i].ring, arr[i].yashe, arr[i].relin = r.h.value, None, 0
+            else:
+                _, y, a, b, c, relin = j
+                arr[i].ring, arr[i].yashe, arr[i].relin = None, y.h.value, 1 if relin else 0
+            arr[i].d_a, arr[i].d_b, arr[i].d_c = _ptr(a), _ptr(b), _ptr(c)
+        h = ctypes.c_void_p()
+        check(lib().cy_mixed_plan_create(arr, len(self._jobs), ctypes.byref(h)), "cy_mixed_plan_create")
+        self.h = h
+
+    def __len__(self) -> int:
+        return len(self._jobs)
+
+    def launch(self, stream=None) -> None:
+        check(lib().cy_mixed_plan_launch(self.h, _stream_handle(stream)), "cy_mixed_plan_launch")
+
+    def status(self, stream=None) -> None:
+        """Raise if a block of the last launch gave up waiting (synchronises)."""
+        check(lib().cy_mixed_plan_status(self.h, _stream_handle(stream)), "cy_mixed_plan_status")
+
+    def status_code(self, stream=None) -> int:
+        return lib().cy_mixed_plan_status(self.h, _stream_handle(stream))
+
+    @property
+    def schedule(self) -> int:
+        v = ctypes.c_int(0)
+        check(lib().cy_mixed_plan_get_schedule(self.h, ctypes.byref(v)), "cy_mixed_plan_get_schedule")
+        return v.value
+
+    @schedule.setter
+    def schedule(self, s: int) -> None:
+        check(lib().cy_mixed_plan_set_schedule(self.h, s), "cy_mixed_plan_set_schedule")
+
+    def autotune(self, stream=None) -> int:
+        check(lib().cy_mixed_plan_autotune(self.h, _stream_handle(stream)), "cy_mixed_plan_autotune")
+        return self.schedule
+
+    def graph(self) -> "Graph":
+        g = ctypes.c_void_p()
+        check(lib().cy_mixed_plan_graph_create(self.h, ctypes.byref(g)), "cy_mixed_plan_graph_create")
+        return Graph(g, self)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().cy_mixed_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
 
 
 def polymul_batched(jobs: Sequence[tuple], stream=None) -> None:
@@ -501,5 +562,5 @@ class Server:
         check(lib().cy_server_reset_stats(self.h), "cy_server_reset_stats")
 
 
-__all__ = ["Server", "Ring", "Yashe", "Workspace", "Graph", "polymul_batched", "polymul_batched_status", "to_limb_array", "from_limb_array", "to_device",
+__all__ = ["Server", "Ring", "Yashe", "Workspace", "Graph", "MixedPlan", "polymul_batched", "polymul_batched_status", "to_limb_array", "from_limb_array", "to_device",
            "to_host", "nlimbs", "CY_OK"]

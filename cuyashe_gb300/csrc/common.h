@@ -72,20 +72,31 @@ struct BasisDev {
     const uint2* ipsi_r[KMAX];
 };
 
-// One product of a mixed batch (different N and q per job) for the persistent
-// kernel k_mixed.
+// One job of a mixed batch (different N and q per job) for the persistent
+// kernel k_mixed: a polynomial product (mode MODQ, no keyswitch) or a YASHE
+// multiply (tensor with the rounding epilogue, then optionally the keyswitch).
 struct MixedJob {
-    const BasisDev* B;  // the job's product basis (mod-q epilogue)
+    const BasisDev* B;   // product / tensor basis
+    const BasisDev* B2;  // keyswitch basis (YASHE with relinearisation), else null
     const uint64_t* a;
     const uint64_t* b;
     uint64_t* c;
-    uint32_t* resid;    // [k][N] residues of this job in the batch scratch
+    uint32_t* resid;     // [max(k, k2)][N] residues of this job in the batch scratch
+    const uint2* evk;    // keyswitch key [ell][k2][N] (NTT domain, Shoup pairs)
     int logn, k, l32, l64;
+    int mode;            // EPI_MODQ (product) or EPI_YASHE (tensor rounding)
+    int centered;        // inputs taken as symmetric representatives (YASHE)
+    int k2, ell;         // keyswitch primes and digits (k2 = 0: none)
+    int n_epi;           // epilogue units of the job (each phase)
+    int need0;           // NTT units' primes the first epilogue waits for (k unless a test starves it)
 };
 
-// A unit of work claimed by one block: kind 0 runs the NTT product of `count`
-// consecutive primes of a job starting at `first`; kind 1 runs the ICRT
-// epilogue of coefficients [first, first + count) once all primes are done.
+// A unit of work claimed by one block: kind 0 runs the forward/pointwise/inverse
+// transforms of `count` consecutive primes of a job starting at `first`; kind 1
+// the job's first epilogue over coefficients [first, first + count) once all
+// its kind-0 primes are done; kind 2 the keyswitch transforms of `count` primes
+// once every kind-1 unit of the job is done; kind 3 the keyswitch's mod-q
+// epilogue once every kind-2 prime is done.
 struct MixedUnit {
     int job, kind, first, count;
 };

@@ -78,6 +78,11 @@ cy_status cy_yashe_mul_graph_create(cy_yashe* y, const uint64_t* d_c1, const uin
         out);
 }
 
+cy_status cy_mixed_plan_graph_create(cy_mixed_plan* plan, cy_graph** out) {
+    if (!plan || !out) return set_error(CY_ERR_INVALID_ARGUMENT, "bad argument");
+    return capture([=](cy_workspace*, cudaStream_t st) { return cy_mixed_plan_launch(plan, st); }, out);
+}
+
 cy_status cy_graph_launch(cy_graph* g, cy_stream_t stream) {
     if (!g || !g->exec) return set_error(CY_ERR_INVALID_ARGUMENT, "graph is NULL");
     CY_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));

@@ -65,6 +65,7 @@ int cy_version(void);
 /* ------------------------------------------------------------------------ */
 
 typedef struct cy_ring cy_ring;
+typedef struct cy_yashe cy_yashe; /* declared with its functions below */
 typedef struct cy_workspace cy_workspace;
 
 typedef struct cy_ring_info {
@@ -163,6 +164,51 @@ cy_status cy_polymul_batched(const cy_polymul_job *jobs, int njobs, cy_stream_t 
  * CY_ERR_TIMEOUT if a block of it gave up waiting for its job's transforms (a
  * bounded wait that cannot expire unless the device stops making progress). */
 cy_status cy_polymul_batched_status(cy_stream_t stream);
+
+/* Prepared mixed batch: a fixed list of polynomial products and YASHE
+ * multiplies (with or without relinearisation) of rings of different N
+ * (1024..8192) and q (up to 192 bits), run as ONE persistent launch: per job
+ * CRT split, forward NTTs, pointwise product, inverse NTT, ICRT with mod q (or
+ * the YASHE rounding round(t/q .)), then for relinearised jobs the word
+ * decomposition, NTT-domain product with the resident evaluation key, inverse
+ * NTT and mod q, all in one kernel over a work list in dependency order.
+ * cy_mixed_plan_create sizes and uploads everything (it allocates and
+ * synchronises); cy_mixed_plan_launch then issues one memset and one kernel on
+ * `stream`, with no allocation and no host synchronisation, so that a caller can
+ * replay it freely (or record it: cy_mixed_plan_graph_create). Results equal
+ * cy_polymul / cy_yashe_mul of each job alone, bit for bit. Outputs must not be
+ * any job's inputs; launches of one plan must not overlap on the GPU (they share
+ * the plan's scratch). The reference multiplies one pair per call and
+ * re-initialises its tables whenever N changes (src/common.h:136-226); its
+ * homomorphic multiply is a chain of such calls (src/ciphertext.cpp:38-130). */
+typedef struct cy_mixed_job {
+    cy_ring *ring;      /* a polynomial product in this ring, or NULL */
+    cy_yashe *yashe;    /* a YASHE multiply of this scheme (keys set), or NULL */
+    int relin;          /* YASHE: relinearise the product */
+    const uint64_t *d_a, *d_b;  /* [N][L] operands (ciphertexts for YASHE) */
+    uint64_t *d_c;      /* [N][L] result */
+} cy_mixed_job;
+typedef struct cy_mixed_plan cy_mixed_plan;
+cy_status cy_mixed_plan_create(const cy_mixed_job *jobs, int njobs, cy_mixed_plan **out);
+cy_status cy_mixed_plan_destroy(cy_mixed_plan *plan);
+cy_status cy_mixed_plan_launch(cy_mixed_plan *plan, cy_stream_t stream);
+/* Synchronises `stream` and reports CY_ERR_TIMEOUT if a block of the last
+ * launch gave up waiting for earlier units of its job (a bounded wait that does
+ * not expire while the device makes progress). */
+cy_status cy_mixed_plan_status(cy_mixed_plan *plan, cy_stream_t stream);
+/* Schedules of the mixed kernel: 0 = 8 coefficients per thread in 1024-thread
+ * blocks, 1 = 16 per thread in 512-thread blocks. The autotuner runs each on the
+ * plan's own buffers (results must agree bit for bit), times it with CUDA
+ * events and keeps the fastest; it synchronises. */
+cy_status cy_mixed_plan_set_schedule(cy_mixed_plan *plan, int schedule);
+cy_status cy_mixed_plan_get_schedule(const cy_mixed_plan *plan, int *schedule);
+cy_status cy_mixed_plan_autotune(cy_mixed_plan *plan, cy_stream_t stream);
+/* For tests of the bounded wait only: makes the first epilogue of job `job`
+ * wait for one more transform than the job has, so that its wait expires after
+ * `spin_limit` back-off steps (about 0.3 us each) and the launch reports
+ * CY_ERR_TIMEOUT through cy_mixed_plan_status. The plan's results are invalid
+ * afterwards. No counterpart in the reference (it has no failure handling). */
+cy_status cy_mixed_plan_test_starve(cy_mixed_plan *plan, int job, unsigned spin_limit);
 
 /* Forward / inverse negacyclic NTT of residue vectors: d_res is [batch][k][N]
  * uint32 residues modulo the ring's CRT primes, transformed in place (values
@@ -434,6 +480,9 @@ cy_status cy_polymul_graph_create(cy_ring *ring, const uint64_t *d_a, const uint
                                   cy_graph **out);
 cy_status cy_yashe_mul_graph_create(cy_yashe *y, const uint64_t *d_c1, const uint64_t *d_c2, uint64_t *d_out,
                                     int batch, int relin, cy_graph **out);
+/* A prepared mixed batch (cy_mixed_plan_launch with the plan's current
+ * schedule) recorded as a graph; the plan must outlive the graph. */
+cy_status cy_mixed_plan_graph_create(cy_mixed_plan *plan, cy_graph **out);
 cy_status cy_graph_launch(cy_graph *graph, cy_stream_t stream);
 cy_status cy_graph_destroy(cy_graph *graph);
 

@@ -67,3 +67,23 @@ def test_single_process_needs_no_group(monkeypatch):
     assert rep.world == 1 and rep.group is None and rep.is_root
     assert replicas.max_over_ranks(rep, 3.5) == 3.5
     replicas.close(rep)
+
+
+def test_bench_gpus_2_launches_two_ranks_on_cpu():
+    """`bench.py --gpus 2` outside a launcher starts two ranks itself
+    (torch.distributed.run); with --cpu-dry-run they use gloo and no CUDA, and
+    rank 0 prints one line for the whole job with n_gpus = 2 and both shares."""
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_PORT")}
+    proc = subprocess.run([sys.executable, "bench.py", "--gpus", "2", "--cpu-dry-run", "--steps", "3",
+                           "--warmup", "3", "--batch", "1000"], cwd=root, env=env, capture_output=True, text=True,
+                          timeout=300)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    lines = [l for l in proc.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1, proc.stdout
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["dry_run"] is True
+    assert d["shards"] == [[0, 1000], [1000, 2000]] and d["pairs_per_step"] == 2000
