@@ -519,7 +519,7 @@ class Server:
         request, or are per-request sequences. Returns the tickets."""
         def addrs(x):
             if hasattr(x, "data_ptr"):
-                step = x[0].numel() * x.element_size() if x.dim() == 3 else 0
+                step = x.stride(0) * x.element_size() if x.dim() == 3 else 0  # 0 for an expanded tensor
                 return [x.data_ptr() + i * step for i in range(x.shape[0] if x.dim() == 3 else 1)]
             return [int(a) for a in x]
         a1, a2, ao = addrs(c1), addrs(c2), addrs(out)

@@ -229,13 +229,15 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
 }
 
 // keyswitch of `batch` polynomials c_j -> out_j (may alias c)
+// chunk_k > 0 sizes the chunks as for a basis of that many primes (the tuner
+// uses the HE multiply's chunks, which are sized by its larger basis).
 static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out,
-                               int batch, Workspace& ws, cudaStream_t st, int variant = -1) {
+                               int batch, Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0) {
     if (batch == 0) return CY_OK;
     const KernelSet& ks =
         kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_KS));
     const int n = B.h.n, k = B.h.k, l64 = B.h.l64;
-    const int chunk = std::min(batch, chunk_jobs(n, k));
+    const int chunk = std::min(batch, chunk_jobs(n, chunk_k > 0 ? std::max(k, chunk_k) : k));
     const int nchunks = (batch + chunk - 1) / chunk;
     int sel = 0;
     CY_TRY(keyswitch_digits_per_pass(ks, ell, &sel));
@@ -352,8 +354,8 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
 }
 
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st, int variant) {
-    return run_keyswitch(B, c, evk, ell, out, batch, ws, st, variant);
+                            Workspace& ws, cudaStream_t st, int variant, int chunk_k) {
+    return run_keyswitch(B, c, evk, ell, out, batch, ws, st, variant, chunk_k);
 }
 
 // Evaluation key in the keyswitch basis, NTT domain, with Shoup companions:

@@ -29,6 +29,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -56,6 +57,7 @@ struct Request {
     uint64_t* h_out = nullptr;
     double t_submit = 0;
     bool done = false;
+    bool taken = false;  // admitted into a batch
     cy_status status = CY_OK;
     size_t bytes = 0;
 };
@@ -136,7 +138,8 @@ struct Slot {
     int cls = -1;
     std::vector<uint64_t> ids;
     size_t bytes = 0;
-    size_t cap_words = 0;  // uint64 words of one output buffer (inputs hold twice as many)
+    size_t cap_words = 0;  // uint64 words of one device output buffer (inputs hold twice as many)
+    size_t cap_host_words = 0;  // the same for the page-locked staging (host-buffer batches)
     uint64_t *d_in = nullptr, *d_out = nullptr, *h_in = nullptr, *h_out = nullptr;
     bool dev = false;            // the batch in flight is of device-resident requests
     size_t cap_ptrs = 0;         // pointer lists of device-resident batches
@@ -166,7 +169,18 @@ struct cy_server {
     std::vector<double> us_per_req;  // per context: running estimate (0: none yet)
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<uint64_t> pending;
+    // pending requests: one FIFO per (context, relin, device-resident) batch key,
+    // and the submission order of all of them (the oldest request's key forms
+    // the next batch; ids already taken are skipped lazily)
+    std::map<int, std::deque<uint64_t>> queues;
+    std::deque<uint64_t> order;
+    size_t n_pending = 0;
+    static int batch_key(const cy::Request& r) { return 4 * r.cls + 2 * r.relin + (r.dev ? 1 : 0); }
+    void enqueue(uint64_t id, const cy::Request& r) {
+        queues[batch_key(r)].push_back(id);
+        order.push_back(id);
+        n_pending++;
+    }
     std::unordered_map<uint64_t, Request> reqs;
     uint64_t next_id = 1;
     std::vector<std::unique_ptr<Slot>> slots;
@@ -193,22 +207,28 @@ static size_t request_bytes(const cy_yashe* y) {
 // capacity is counted in words, not polynomials.
 // Growing frees and allocates (cudaFree waits for the whole device), so a slot
 // grows to twice what the batch needs: few growths once the load settles.
-static cy_status grow_slot(Slot& s, size_t polys, size_t poly_words) {
+static cy_status grow_slot(Slot& s, size_t polys, size_t poly_words, bool host) {
     const size_t need = polys * poly_words;
-    if (need <= s.cap_words) return CY_OK;
-    const size_t words = std::max(2 * need, 2 * s.cap_words);
-    if (s.d_in) cudaFree(s.d_in);
-    if (s.d_out) cudaFree(s.d_out);
-    if (s.h_in) cudaFreeHost(s.h_in);
-    if (s.h_out) cudaFreeHost(s.h_out);
-    s.d_in = s.d_out = s.h_in = s.h_out = nullptr;
-    s.cap_words = 0;
-    const size_t bytes = words * sizeof(uint64_t);
-    CY_CUDA(cudaMalloc(&s.d_in, 2 * bytes));
-    CY_CUDA(cudaMalloc(&s.d_out, bytes));
-    CY_CUDA(cudaMallocHost(&s.h_in, 2 * bytes));
-    CY_CUDA(cudaMallocHost(&s.h_out, bytes));
-    s.cap_words = words;
+    if (need > s.cap_words) {  // device buffers
+        const size_t words = std::max(2 * need, 2 * s.cap_words);
+        if (s.d_in) cudaFree(s.d_in);
+        if (s.d_out) cudaFree(s.d_out);
+        s.d_in = s.d_out = nullptr;
+        s.cap_words = 0;
+        CY_CUDA(cudaMalloc(&s.d_in, 2 * words * sizeof(uint64_t)));
+        CY_CUDA(cudaMalloc(&s.d_out, words * sizeof(uint64_t)));
+        s.cap_words = words;
+    }
+    if (host && need > s.cap_host_words) {  // page-locked staging: host-buffer batches only
+        const size_t words = std::max(2 * need, 2 * s.cap_host_words);
+        if (s.h_in) cudaFreeHost(s.h_in);
+        if (s.h_out) cudaFreeHost(s.h_out);
+        s.h_in = s.h_out = nullptr;
+        s.cap_host_words = 0;
+        CY_CUDA(cudaMallocHost(&s.h_in, 2 * words * sizeof(uint64_t)));
+        CY_CUDA(cudaMallocHost(&s.h_out, words * sizeof(uint64_t)));
+        s.cap_host_words = words;
+    }
     return CY_OK;
 }
 
@@ -252,7 +272,8 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         }
         const cy_yashe* y = S->classes[s.cls];
         d.poly = (size_t)y->ring->n * y->ring->l64;
-        if (s.ids.size() * d.poly > s.cap_words) d.st = set_error(CY_ERR_INTERNAL, "serving slot too small");
+        if (s.ids.size() * d.poly > (s.dev ? s.cap_words : s.cap_host_words))
+            d.st = set_error(CY_ERR_INTERNAL, "serving slot too small");
         if (!s.dev)  // device-resident results are already in the callers' buffers
             for (uint64_t id : s.ids) d.outs.push_back(S->reqs[id].h_out);
         done.push_back(std::move(d));
@@ -287,10 +308,18 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
     // 2. new batches on free slots: choose under the lock, stage and launch without it
     for (auto& sp : S->slots) {
         Slot& s = *sp;
-        if (s.busy || S->pending.empty()) continue;
-        const int cls = S->reqs[S->pending.front()].cls;
-        const int relin = S->reqs[S->pending.front()].relin;
-        const bool dev = S->reqs[S->pending.front()].dev;
+        if (s.busy || S->n_pending == 0) continue;
+        while (!S->order.empty()) {  // drop ids already admitted (or already waited for)
+            auto f = S->reqs.find(S->order.front());
+            if (f != S->reqs.end() && !f->second.taken) break;
+            S->order.pop_front();
+        }
+        if (S->order.empty()) continue;
+        const Request& oldest = S->reqs[S->order.front()];
+        const int cls = oldest.cls;
+        const int relin = oldest.relin;
+        const bool dev = oldest.dev;
+        std::deque<uint64_t>& q = S->queues[cy_server::batch_key(oldest)];
         cy_yashe* y = S->classes[cls];
         const size_t per = request_bytes(y);
         int cap = S->cfg.max_batch;  // requests of this batch
@@ -300,19 +329,17 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         std::vector<const uint64_t*> in1, in2;
         std::vector<uint64_t*> outs;
         size_t bytes = 0;
-        for (auto it = S->pending.begin(); it != S->pending.end() && (int)take.size() < cap;) {
-            const Request& r = S->reqs[*it];
-            if (r.cls != cls || r.relin != relin || r.dev != dev) {
-                ++it;
-                continue;
-            }
+        while (!q.empty() && (int)take.size() < cap) {
+            Request& r = S->reqs[q.front()];
             if (S->in_use + bytes + per > S->cfg.device_budget_bytes) break;  // admission by device memory
-            take.push_back(*it);
+            take.push_back(q.front());
             in1.push_back(r.h_c1);
             in2.push_back(r.h_c2);
             outs.push_back(r.h_out);
+            r.taken = true;
             bytes += per;
-            it = S->pending.erase(it);
+            q.pop_front();
+            S->n_pending--;
         }
         if (take.empty()) break;  // the budget is full until a batch retires
         s.busy = true;  // reserved: not retired before its event is recorded below
@@ -326,8 +353,9 @@ static void dispatch_once(cy_server* S, std::unique_lock<std::mutex>& lock) {
         lock.unlock();
         const int nb = (int)take.size();
         const size_t poly = (size_t)y->ring->n * y->ring->l64;
-        cy_status st = grow_slot(s, nb, poly);
-        if (st == CY_OK && (size_t)nb * poly > s.cap_words) st = set_error(CY_ERR_INTERNAL, "serving slot too small");
+        cy_status st = grow_slot(s, nb, poly, !dev);
+        if (st == CY_OK && ((size_t)nb * poly > s.cap_words || (!dev && (size_t)nb * poly > s.cap_host_words)))
+            st = set_error(CY_ERR_INTERNAL, "serving slot too small");
         if (st == CY_OK && dev) {
             // device-resident: pointer lists in, gather, multiply, scatter
             st = grow_ptrs(s, 3 * (size_t)nb);
@@ -391,7 +419,7 @@ static void worker_loop(cy_server* S) {
         dispatch_once(S, lock);
         bool busy = false;
         for (auto& s : S->slots) busy |= s->busy;
-        if (busy || !S->pending.empty()) {
+        if (busy || S->n_pending > 0) {
             // poll the slots' events without holding the lock
             lock.unlock();
             std::this_thread::sleep_for(std::chrono::microseconds(S->cfg.poll_us));
@@ -479,7 +507,7 @@ cy_status cy_server_submit(cy_server* S, const cy_serve_request* req, uint64_t* 
     if (S->t_first == 0) S->t_first = r.t_submit;
     const uint64_t id = S->next_id++;
     S->reqs[id] = r;
-    S->pending.push_back(id);
+    S->enqueue(id, r);
     *ticket = id;
     S->cv_work.notify_one();
     return CY_OK;
@@ -515,7 +543,7 @@ cy_status cy_server_submit_device(cy_server* S, const cy_serve_request_dev* reqs
         if (S->t_first == 0) S->t_first = t;
         const uint64_t id = S->next_id++;
         S->reqs[id] = r;
-        S->pending.push_back(id);
+        S->enqueue(id, r);
         tickets[i] = id;
     }
     S->cv_work.notify_one();
@@ -548,7 +576,7 @@ cy_status cy_server_drain(cy_server* S, int timeout_ms) {
     if (!S) return set_error(CY_ERR_INVALID_ARGUMENT, "NULL argument");
     std::unique_lock<std::mutex> lock(S->mu);
     const bool ok = S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), [&] {
-        if (!S->pending.empty()) return false;
+        if (S->n_pending > 0) return false;
         for (auto& s : S->slots)
             if (s->busy) return false;
         return true;

@@ -12,6 +12,7 @@
 // (src/cuda_bn.cu:983-988, 1014-1019).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -29,7 +30,7 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
                           cudaStream_t st, int variant);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st, int variant);
+                            Workspace& ws, cudaStream_t st, int variant, int chunk_k);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 
 cy_status run_ntt_api(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st, int variant);
@@ -167,7 +168,10 @@ static cy_status tune_product(const Basis& B, bool centered, int batch, cudaStre
                    &chosen);
 }
 
-static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, int batch, cudaStream_t st) {
+// chunk_k: the prime count that sizes the HE multiply's chunks (its larger basis),
+// so that each schedule is timed on the launches the multiply makes.
+static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, int batch, cudaStream_t st,
+                                int chunk_k) {
     const int n = relin.h.n, l64 = relin.h.l64;
     const size_t bytes = sizeof(uint64_t) * (size_t)batch * n * l64;
     std::vector<uint64_t> hc = random_polys(batch, n, l64, relin.h.qbits, 3);
@@ -180,7 +184,7 @@ static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, i
     return tune_op(relin.h.logn, l64, TUNE_KS, bytes, st,
                    [&](int v, void* out) {
                        return run_keyswitch_api(relin, (const uint64_t*)c.p, evk, ell, (uint64_t*)out, batch, ws, st,
-                                                v);
+                                                v, chunk_k);
                    },
                    &chosen);
 }
@@ -236,7 +240,7 @@ cy_status cy_yashe_autotune(cy_yashe* y, int batch, cy_stream_t stream) {
         CY_TRY(prepare_evk(y->relin, h.data(), y->ell, r->n, r->l64, &tmp));
         evk = tmp;
     }
-    cy_status s = tune_keyswitch(y->relin, evk, y->ell, batch, st);
+    cy_status s = tune_keyswitch(y->relin, evk, y->ell, batch, st, std::max(y->tensor.h.k, y->relin.h.k));
     if (tmp) cudaFree(tmp);
     return s;
 }
