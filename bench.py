@@ -1007,10 +1007,11 @@ def run_ours(args):
     replicas.close(rep)
 
 
-def ncu_schedules(batch: int = 256):
+def ncu_schedules(batch: int = 1024, only: str = "all"):
     """One call of every N = 4096 schedule of the product (plain and centred),
     the keyswitch and the standalone NTT (forced with cy_tuning_import) between
-    cudaProfilerStart/Stop, for ncu's per-schedule counts; prints the order."""
+    cudaProfilerStart/Stop, for ncu's per-schedule counts; prints the order.
+    `only`: "all", or a comma-separated list such as "mulc=7,ks=5,ntt=9"."""
     import numpy as np
     import torch
 
@@ -1038,6 +1039,9 @@ def ncu_schedules(batch: int = 256):
     O = Y.ring.empty(batch)
     RES = torch.zeros((batch, R.k, N), dtype=torch.int32, device="cuda")
     plan = [(op, v) for op in ("mul", "mulc", "ks", "ntt") for v in variants(op)]
+    if only != "all":
+        want = {tuple(x.split("=")) for x in only.split(",")}
+        plan = [(op, v) for op, v in plan if (op, str(v)) in want]
 
     def run(op, v):
         cy.tuning_import("n%d.l2.%s=%d" % (N, op, v))
@@ -1129,8 +1133,9 @@ def main():
                     help="set up, warm up, run one step inside cudaProfilerStart/Stop, exit (for ncu)")
     ap.add_argument("--ncu-deep", type=int, default=0, metavar="PAIRS",
                     help="the same for one autotuned deep-level step (N=16384, 380-bit q) of PAIRS pairs")
-    ap.add_argument("--ncu-schedules", action="store_true",
-                    help="one call of every N=4096 schedule inside cudaProfilerStart/Stop, exit (for ncu)")
+    ap.add_argument("--ncu-schedules", nargs="?", const="all", default=None, metavar="LIST",
+                    help="one call of every N=4096 schedule (or of LIST, e.g. mulc=7,ks=5,ntt=9) inside "
+                         "cudaProfilerStart/Stop, exit (for ncu)")
     ap.add_argument("--cpu-dry-run", action="store_true",
                     help="ranks and shares only, without CUDA (tests of the multi-GPU launcher)")
     args = ap.parse_args()
@@ -1143,8 +1148,8 @@ def main():
     if args.warmup < 3 and args.impl == "ours":
         log("note: warm-up raised to 3")
         args.warmup = 3
-    if args.ncu_schedules:
-        ncu_schedules()
+    if args.ncu_schedules is not None:
+        ncu_schedules(only=args.ncu_schedules)
     elif args.impl == "reference":
         run_reference(args)
     elif args.serving_only > 0:
