@@ -127,13 +127,15 @@ bool mixed_supported(const cy_ring* r);
 // scratch. Chunk c runs on lane c mod lanes (one chunk's kernels fill the tails
 // of the others'); begin() orders the side streams after the caller's work,
 // end() orders the caller's stream after theirs. The lane count is
-// CY_CHUNK_LANES (1 .. 1 + kMaxSide, default 2); cy_set_chunk_overlap(0) makes it 1.
+// CY_CHUNK_LANES (1 .. 1 + kMaxSide, default 3: measured 3.01-3.04 ms per 4096-pair
+// HE multiply step against 3.08 with two lanes and 3.62 with one); cy_set_chunk_overlap(0)
+// makes it 1.
 static std::atomic<int> g_two_lanes{1};
 
 static int lane_count() {
     static const int v = [] {
         const char* e = std::getenv("CY_CHUNK_LANES");
-        const int x = e ? std::atoi(e) : 2;
+        const int x = e ? std::atoi(e) : 3;
         return x < 1 ? 1 : (x > 1 + kMaxSide ? 1 + kMaxSide : x);
     }();
     return g_two_lanes.load() ? v : 1;

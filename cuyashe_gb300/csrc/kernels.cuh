@@ -149,11 +149,18 @@ __device__ __forceinline__ uint32_t crt_words(const uint32_t (&w)[W], const uint
         if constexpr (W == 2) {
             gt = ((uint64_t)w[1] << 32 | w[0]) > ((uint64_t)qh[1] << 32 | qh[0]);
         } else if constexpr (W == 4) {
-            const unsigned __int128 xv = (unsigned __int128)((uint64_t)w[3] << 32 | w[2]) << 64 |
-                                         ((uint64_t)w[1] << 32 | w[0]);
-            const unsigned __int128 hv = (unsigned __int128)((uint64_t)qh[3] << 32 | qh[2]) << 64 |
-                                         ((uint64_t)qh[1] << 32 | qh[0]);
-            gt = xv > hv;
+            // (q-1)/2 - x borrows exactly when x > (q-1)/2: one subtract-with-borrow
+            // chain, its final borrow spread to a mask (no compares, no selects)
+            uint32_t mask;
+            asm("{\n\t.reg .u32 d;\n\t"
+                "sub.cc.u32 d, %1, %5;\n\t"
+                "subc.cc.u32 d, %2, %6;\n\t"
+                "subc.cc.u32 d, %3, %7;\n\t"
+                "subc.cc.u32 d, %4, %8;\n\t"
+                "subc.u32 %0, 0, 0;\n\t}"
+                : "=r"(mask)
+                : "r"(qh[0]), "r"(qh[1]), "r"(qh[2]), "r"(qh[3]), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]));
+            return acc + (mask & (2 * c.p - c.qmodp));  // [0, 4p)
         } else {
             gt = w[W - 1] > qh[W - 1];
             if (w[W - 1] == qh[W - 1]) {
