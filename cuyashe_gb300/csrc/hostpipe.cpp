@@ -3,11 +3,11 @@
 // The reference moves every operand to the device before a product and back
 // after it, synchronously (Polynomial::update_device_data / update_host_data,
 // src/polynomial.cpp:265-417; cudaDeviceSynchronize, src/common.h:223). Here a
-// host-buffer call is cut into chunks that flow through three slots of device
-// buffers: while chunk c runs its kernels, chunk c+1 is copied in and chunk c-1
-// is copied out, on a copy-in stream, two kernel streams (chunks alternate
-// between them so that neighbouring chunks' kernels overlap) and a copy-out
-// stream. With page-locked host buffers the copies run on the copy engines
+// host-buffer call is cut into chunks that flow through six slots of device
+// buffers: while chunks run their kernels, the next ones are copied in and the
+// previous ones copied out, on a copy-in stream, three kernel streams (chunks are
+// dealt round-robin so that neighbouring chunks' kernels overlap, as the lanes of
+// the device-buffer calls do) and a copy-out stream. With page-locked host buffers the copies run on the copy engines
 // alongside the kernels; pageable buffers give the same result, with copies
 // that do not overlap.
 #include <cuda_runtime.h>
@@ -21,20 +21,21 @@
 
 namespace cy {
 
-constexpr int kPipeSlots = 3;
+constexpr int kPipeSlots = 6;  // chunks in flight (copy in, kernels, copy out)
+constexpr int kRunStreams = 3;
 
 // Per-device pipeline state, kept until process exit. Calls on one device take
 // the pipeline in turn (the host blocks until a call's last copy is done).
 struct HostPipe {
     std::mutex mu;
-    cudaStream_t s_in = nullptr, s_run[2] = {nullptr, nullptr}, s_out = nullptr;
+    cudaStream_t s_in = nullptr, s_run[kRunStreams] = {}, s_out = nullptr;
     struct Slot {
         uint64_t* d = nullptr;  // in0 | in1 | out, `words` each
         size_t words = 0;
         cudaEvent_t in_done = nullptr, run_done = nullptr, out_done = nullptr;
         bool used = false;
     } slot[kPipeSlots];
-    cy_workspace ws[2];  // one per kernel stream
+    cy_workspace ws[kRunStreams];  // one per kernel stream
 };
 
 static HostPipe& host_pipe(int dev) {
@@ -48,10 +49,9 @@ static HostPipe& host_pipe(int dev) {
 
 static cy_status pipe_init(HostPipe& P, int dev) {
     if (P.s_in) return CY_OK;
-    P.ws[0].ws.device = P.ws[1].ws.device = dev;
+    for (auto& w : P.ws) w.ws.device = dev;
     CY_CUDA(cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking));
-    CY_CUDA(cudaStreamCreateWithFlags(&P.s_run[0], cudaStreamNonBlocking));
-    CY_CUDA(cudaStreamCreateWithFlags(&P.s_run[1], cudaStreamNonBlocking));
+    for (auto& r : P.s_run) CY_CUDA(cudaStreamCreateWithFlags(&r, cudaStreamNonBlocking));
     CY_CUDA(cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking));
     for (auto& s : P.slot) {
         CY_CUDA(cudaEventCreateWithFlags(&s.in_done, cudaEventDisableTiming));
@@ -131,11 +131,11 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
             e = cudaMemcpyAsync(in1, h_in1 + off, bytes, cudaMemcpyHostToDevice, P.s_in);
         if (e == cudaSuccess) e = cudaEventRecord(S.in_done, P.s_in);
         // run once the inputs are in and the slot's previous output is out
-        cudaStream_t run = P.s_run[c & 1];
+        cudaStream_t run = P.s_run[c % kRunStreams];
         if (e == cudaSuccess) e = cudaStreamWaitEvent(run, S.in_done, 0);
         if (e == cudaSuccess && S.used) e = cudaStreamWaitEvent(run, S.out_done, 0);
         if (e != cudaSuccess) break;
-        st = op(&P.ws[c & 1], in0, h_in1 ? in1 : nullptr, out, nj, run);
+        st = op(&P.ws[c % kRunStreams], in0, h_in1 ? in1 : nullptr, out, nj, run);
         if (st != CY_OK) break;
         e = cudaEventRecord(S.run_done, run);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_out, S.run_done, 0);
@@ -145,9 +145,11 @@ cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* 
     }
     // drain every stream, whatever happened above
     const cudaError_t e1 = cudaStreamSynchronize(P.s_in);
-    cudaError_t e2 = cudaStreamSynchronize(P.s_run[0]);
-    const cudaError_t e2b = cudaStreamSynchronize(P.s_run[1]);
-    if (e2 == cudaSuccess) e2 = e2b;
+    cudaError_t e2 = cudaSuccess;
+    for (auto& r : P.s_run) {
+        const cudaError_t e2b = cudaStreamSynchronize(r);
+        if (e2 == cudaSuccess) e2 = e2b;
+    }
     const cudaError_t e3 = cudaStreamSynchronize(P.s_out);
     if (st != CY_OK) return st;
     if (e != cudaSuccess) return cuda_error(e, "host pipeline");
