@@ -462,7 +462,9 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G)
 // nearby instructions (the unrolled transform is larger than the instruction
 // cache). Jobs past the last are computed on the last job and not stored.
 // --------------------------------------------------------------------------
-template <int LOGN, int LOGE, bool INV, int MINB = 0, bool COAL = false, int TPB = 1>
+// LOOP (N = 4096, E = 64): the two passes run as a loop over one copy of the pass
+// code (ntt_core.cuh, ntt64_forward / ntt64_inverse).
+template <int LOGN, int LOGE, bool INV, int MINB = 0, bool COAL = false, int TPB = 1, bool LOOP = false>
 __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB : 1))
     k_ntt1(const BasisDev* __restrict__ B, uint32_t* __restrict__ res, const uint32_t* __restrict__ ninv,
            int njobs) {
@@ -490,8 +492,9 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
     constexpr bool VEC = PL::LOGD(LAST) == 0 && PL::R(LAST) == PL::LOGE && E % 4 == 0;
     if (!INV) {
 #pragma unroll
-        for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, 0>(tau, e)];
-        ntt_forward<PL, 1>(x, B->psi[prime], m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
+        for (int e = 0; e < E; e++) x[0][e] = COAL ? __ldcs(v + slot_pos<PL, 0>(tau, e)) : v[slot_pos<PL, 0>(tau, e)];
+        if constexpr (LOOP) ntt64_forward<PL, 1>(x, B->psi[prime], B->psi_r[prime], m, tau, smem);
+        else ntt_forward<PL, 1>(x, B->psi[prime], m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
         if constexpr (COAL) {
             // row tau (positions 64 tau + u) into the padded region (word 65 tau + u),
             // then column tau (positions tau + 64 m, word 65 m + tau) to global memory
@@ -501,7 +504,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
             __syncthreads();
             if (store) {
 #pragma unroll
-                for (int m = 0; m < E; m++) v[tau + 64 * m] = smem[tau + 65 * m];
+                for (int m = 0; m < E; m++) __stcs(v + tau + 64 * m, smem[tau + 65 * m]);
             }
         } else if constexpr (VEC) {
             if (store) {
@@ -521,7 +524,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
             // columns in (coalesced), rows out of the padded region; the exchange
             // of the inverse then reuses the region after a barrier (stride 0)
 #pragma unroll
-            for (int m = 0; m < E; m++) smem[tau + 65 * m] = v[tau + 64 * m];
+            for (int m = 0; m < E; m++) smem[tau + 65 * m] = __ldcs(v + tau + 64 * m);
             __syncthreads();
 #pragma unroll
             for (int u = 0; u < E; u++) x[0][u] = smem[65 * tau + u];
@@ -541,11 +544,17 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G * TPB, (MINB > 0 ? MINB
             for (int e = 0; e < E; e++) x[0][e] = v[slot_pos<PL, LAST>(tau, e)];
         }
         // N^-1 is applied inside the last stage (outputs in [0, p))
-        ntt_inverse<PL, 1>(x, B->ipsi[prime], m, tau, smem, stride, 0, CtaSync(), 1, B->ipsi_r[prime],
-                           ninv + 4 * prime);
+        if constexpr (LOOP)
+            ntt64_inverse<PL, 1>(x, B->ipsi[prime], B->ipsi_r[prime], m, tau, smem, stride == 0, ninv + 4 * prime);
+        else
+            ntt_inverse<PL, 1>(x, B->ipsi[prime], m, tau, smem, stride, 0, CtaSync(), 1, B->ipsi_r[prime],
+                               ninv + 4 * prime);
         if (store) {
 #pragma unroll
-            for (int e = 0; e < E; e++) v[slot_pos<PL, 0>(tau, e)] = x[0][e];
+            for (int e = 0; e < E; e++) {
+                if constexpr (COAL) __stcs(v + slot_pos<PL, 0>(tau, e), x[0][e]);
+                else v[slot_pos<PL, 0>(tau, e)] = x[0][e];
+            }
         }
     }
 }
@@ -1090,10 +1099,11 @@ void fill_kernel_set(KernelSet& ks) {
     if constexpr (SPECIALISE && (SPEC_MASK & 64u))
         fill_l64<LOGN, LOGE, 6, MB_MUL, MB_KS, SINGLE_KS, SINGLE_MUL, ND_LO, ND_HI>(ks);
     if constexpr (LOGE >= 6) {  // one transform per block (k_ntt1), coalesced row side at N = 4096
-        // register budgets measured best at N = 4096: 128 (forward), 96 (inverse)
+        // N = 4096: coalesced row side, the two passes as a loop over one copy of the
+        // pass code, 96 registers (10 blocks per SM), measured best in both directions
         constexpr bool COAL = LOGN == 12 && LOGE == 6;
-        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false, 8, COAL>;
-        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true, 10, COAL>;
+        ks.ntt[0] = (void*)k_ntt1<LOGN, LOGE, false, 10, COAL, 1, COAL>;
+        ks.ntt[1] = (void*)k_ntt1<LOGN, LOGE, true, 10, COAL, 1, COAL>;
         ks.ntt_jobs_per_block = 1;
     } else {
         ks.ntt[0] = (void*)k_ntt<LOGN, LOGE, false>;

@@ -312,4 +312,117 @@ __device__ __forceinline__ int ntt_inverse(uint32_t (&x)[NOPS][PL::E], const uin
     return InvFrom<PL, PL::NPASS - 2, NOPS, Sync>::run(x, tw, m, tau, sm, stride, buf, bar, tm, twr, scale);
 }
 
+// ---------------------------------------------------------------------------
+// Two-pass transforms of 64 coefficients per thread (N = 4096) with ONE copy of
+// the pass code: both passes pair the same register slots at every stage (slot
+// u with u + 2^(5-l)); only their twiddles differ (the first pass's are the same
+// for every thread, the row pass's come from the lane-ordered table). The passes
+// therefore run as two iterations of a loop that is not unrolled, with the
+// twiddle pointers of the iteration in registers: half the instructions of the
+// unrolled transform in the instruction cache.
+// twp[l]: twiddle 0 of stage l (pairs (h, h+1) start there for l >= 1);
+// tws: distance in uint2 between consecutive pairs (2, or 2G in the rows table).
+template <int NOPS>
+__device__ __forceinline__ uint2 tw_dyn(const uint2* __restrict__ base, int h, int l, int tws) {
+    if (l == 0) return __ldg(base);
+    const uint4 W2 = __ldg(reinterpret_cast<const uint4*>(base + (h >> 1) * tws));
+    return (h & 1) ? make_uint2(W2.z, W2.w) : make_uint2(W2.x, W2.y);
+}
+
+template <int NOPS>
+__device__ __forceinline__ void fwd_pass64(uint32_t (&x)[NOPS][64], const uint2* const (&twp)[6], int tws,
+                                           const Mod& m) {
+#pragma unroll
+    for (int l = 0; l < 6; l++) {
+        const int half = 1 << (5 - l);
+        uint2 W = make_uint2(0u, 0u);
+#pragma unroll
+        for (int b = 0; b < 32; b++) {
+            const int h = b >> (5 - l), j = b & (half - 1);
+            if (j == 0) W = tw_dyn<NOPS>(twp[l], h, l, tws);
+            const int u = (h << (6 - l)) + j;
+#pragma unroll
+            for (int o = 0; o < NOPS; o++) ct_bfly(x[o][u], x[o][u + half], W.x, W.y, m);
+        }
+    }
+}
+
+template <int NOPS>
+__device__ __forceinline__ void inv_pass64(uint32_t (&x)[NOPS][64], const uint2* const (&twp)[6], int tws,
+                                           const Mod& m, const uint32_t* __restrict__ scale) {
+#pragma unroll
+    for (int l = 5; l >= 0; l--) {
+        const int half = 1 << (5 - l);
+        if (l == 0 && scale != nullptr) {  // the transform's last stage with N^-1 folded in
+            const uint32_t n0 = __ldg(scale), n0s = __ldg(scale + 1), n1 = __ldg(scale + 2), n1s = __ldg(scale + 3);
+#pragma unroll
+            for (int u = 0; u < 32; u++)
+#pragma unroll
+                for (int o = 0; o < NOPS; o++) {
+                    uint32_t& X = x[o][u];
+                    uint32_t& Y = x[o][u + 32];
+                    const uint32_t sv = shoup_m(X + Y, n0, n0s, m);
+                    const uint32_t dv = shoup_m(X - Y + m.p2, n1, n1s, m);
+                    X = __viaddmin_u32(sv, m.np, sv);
+                    Y = __viaddmin_u32(dv, m.np, dv);
+                }
+            continue;
+        }
+        uint2 W = make_uint2(0u, 0u);
+#pragma unroll
+        for (int b = 0; b < 32; b++) {
+            const int h = b >> (5 - l), j = b & (half - 1);
+            if (j == 0) W = tw_dyn<NOPS>(twp[l], h, l, tws);
+            const int u = (h << (6 - l)) + j;
+#pragma unroll
+            for (int o = 0; o < NOPS; o++) gs_bfly(x[o][u], x[o][u + half], W.x, W.y, m);
+        }
+    }
+}
+
+// twiddle pointers of pass `pass` (0: column pass, shared by all threads; 1: row
+// pass, lane-ordered table) of a transform of 4096 with 64 threads
+__device__ __forceinline__ void pass64_twiddles(int pass, const uint2* __restrict__ tw, const uint2* __restrict__ twr,
+                                                int tau, const uint2* (&twp)[6], int& tws) {
+#pragma unroll
+    for (int l = 0; l < 6; l++)
+        twp[l] = pass == 0 ? tw + (1 << l) : twr + 64 * ((1 << l) - 1) + (l == 0 ? tau : 2 * tau);
+    tws = pass == 0 ? 2 : 128;
+}
+
+// Forward transform, registers in column layout (positions tau + 64 u) ->
+// row layout (64 tau + u); exchange region `sm` (one, SMW = 4160 words per operand).
+template <class PL, int NOPS>
+__device__ __forceinline__ void ntt64_forward(uint32_t (&x)[NOPS][64], const uint2* __restrict__ tw,
+                                              const uint2* __restrict__ twr, const Mod& m, int tau, uint32_t* sm) {
+    static_assert(PL::LOGN == 12 && PL::LOGE == 6, "two passes of six stages");
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        const uint2* twp[6];
+        int tws;
+        pass64_twiddles(pass, tw, twr, tau, twp, tws);
+        fwd_pass64<NOPS>(x, twp, tws, m);
+        if (pass == 0) exchange<PL, 0, 1, NOPS>(x, sm, tau, false);
+    }
+}
+
+// Inverse transform, row layout -> column layout; `sync_before`: a barrier
+// before the exchange's writes (the region was read just before); scale as in
+// inv_pass (or null).
+template <class PL, int NOPS>
+__device__ __forceinline__ void ntt64_inverse(uint32_t (&x)[NOPS][64], const uint2* __restrict__ tw,
+                                              const uint2* __restrict__ twr, const Mod& m, int tau, uint32_t* sm,
+                                              bool sync_before, const uint32_t* __restrict__ scale) {
+    static_assert(PL::LOGN == 12 && PL::LOGE == 6, "two passes of six stages");
+#pragma unroll 1
+    for (int it = 0; it < 2; it++) {
+        const int pass = 1 - it;
+        const uint2* twp[6];
+        int tws;
+        pass64_twiddles(pass, tw, twr, tau, twp, tws);
+        inv_pass64<NOPS>(x, twp, tws, m, pass == 0 ? scale : nullptr);
+        if (pass == 1) exchange<PL, 1, 0, NOPS>(x, sm, tau, sync_before);
+    }
+}
+
 }  // namespace cy
