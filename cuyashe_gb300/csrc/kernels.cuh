@@ -250,11 +250,17 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
         }
     }
     constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, 2>();
-    int buf = ntt_forward<PL, 2>(x, psi, c.m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
+    // 64 coefficients per thread at N = 4096: both transforms loop over one copy of
+    // the pass code (the unrolled three transforms overflow the instruction cache)
+    constexpr bool LOOP64 = LOGN == 12 && LOGE == 6;
+    int buf = 0;
+    if constexpr (LOOP64) ntt64_forward<PL, 2>(x, psi, B->psi_r[prime], c.m, tau, smem);
+    else buf = ntt_forward<PL, 2>(x, psi, c.m, tau, smem, STRIDE, 0, CtaSync(), 1, B->psi_r[prime]);
     uint32_t z[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) z[0][e] = mont(red(x[0][e], 2 * c.p), red(x[1][e], 2 * c.p), c.p, c.pinv);
-    ntt_inverse<PL, 1>(z, ipsi, c.m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
+    if constexpr (LOOP64) ntt64_inverse<PL, 1>(z, ipsi, B->ipsi_r[prime], c.m, tau, smem + STRIDE, STRIDE == 0, nullptr);
+    else ntt_inverse<PL, 1>(z, ipsi, c.m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = z[0][e];
@@ -329,7 +335,12 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
                 }
             }
         }
-        buf = ntt_forward<PL, ND>(x, psi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->psi_r[prime]);
+        if constexpr (LOGN == 12 && LOGE == 6) {  // one copy of the pass code (see k_mul)
+            ntt64_forward<PL, ND>(x, psi, B->psi_r[prime], m, tau, smem, true);
+            buf++;
+        } else {
+            buf = ntt_forward<PL, ND>(x, psi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->psi_r[prime]);
+        }
 #pragma unroll
         for (int o = 0; o < ND; o++) {
             const int d = d0 + o;
@@ -364,7 +375,8 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
             }
         }
     }
-    ntt_inverse<PL, 1>(acc, ipsi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
+    if constexpr (LOGN == 12 && LOGE == 6) ntt64_inverse<PL, 1>(acc, ipsi, B->ipsi_r[prime], m, tau, smem, true, nullptr);
+    else ntt_inverse<PL, 1>(acc, ipsi, m, tau, smem, STRIDE, buf, CtaSync(), 1, B->ipsi_r[prime]);
     uint32_t* out = resid + ((size_t)job * k + prime) * PL::N;
 #pragma unroll
     for (int e = 0; e < E; e++) out[slot_pos<PL, 0>(tau, e)] = acc[0][e];

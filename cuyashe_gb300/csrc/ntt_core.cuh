@@ -394,7 +394,8 @@ __device__ __forceinline__ void pass64_twiddles(int pass, const uint2* __restric
 // row layout (64 tau + u); exchange region `sm` (one, SMW = 4160 words per operand).
 template <class PL, int NOPS>
 __device__ __forceinline__ void ntt64_forward(uint32_t (&x)[NOPS][64], const uint2* __restrict__ tw,
-                                              const uint2* __restrict__ twr, const Mod& m, int tau, uint32_t* sm) {
+                                              const uint2* __restrict__ twr, const Mod& m, int tau, uint32_t* sm,
+                                              bool sync_before = false) {
     static_assert(PL::LOGN == 12 && PL::LOGE == 6, "two passes of six stages");
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
@@ -402,7 +403,7 @@ __device__ __forceinline__ void ntt64_forward(uint32_t (&x)[NOPS][64], const uin
         int tws;
         pass64_twiddles(pass, tw, twr, tau, twp, tws);
         fwd_pass64<NOPS>(x, twp, tws, m);
-        if (pass == 0) exchange<PL, 0, 1, NOPS>(x, sm, tau, false);
+        if (pass == 0) exchange<PL, 0, 1, NOPS>(x, sm, tau, sync_before);
     }
 }
 
