@@ -137,6 +137,8 @@ SIGNATURES = {
     "cy_mixed_plan_test_starve": ([_vp, _i, ctypes.c_uint], _i),
     "cy_mixed_plan_graph_create": ([_vp, ctypes.POINTER(_vp)], _i),
     "cy_ntt": ([_vp, _vp, _i, _i, _vp], _i),
+    "cy_ntt_check": ([], _i),
+    "cy_ntt_test_wait": ([ctypes.c_uint, ctypes.c_uint], _i),
     "cy_crt": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_icrt": ([_vp, _vp, _vp, _i, _vp], _i),
     "cy_yashe_create": ([ctypes.POINTER(YasheParams), ctypes.POINTER(_vp)], _i),

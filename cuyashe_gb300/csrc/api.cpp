@@ -299,6 +299,17 @@ static cy_status run_ntt(const Basis& B, uint32_t* res, int batch, bool inverse,
         kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_NTT));
     const BasisDev* Bd = B.d;
     const uint32_t* ninv = B.d_ninv;
+    const long long rows = (long long)batch * B.h.k * (B.h.n / 64);
+    if (inverse && ks.intt_tma && B.h.logn == 12 && ntt_tma_usable(res, rows)) {  // input tiles by TMA
+        alignas(64) CUtensorMap map;
+        dim3 grid;
+        int* err = nullptr;
+        CY_TRY(intt_tma_prepare(res, rows, B.h.k, batch, &map, &grid, &err));
+        uint32_t spin = ntt_tma_spin_limit(), extra = ntt_tma_extra_tx();
+        void* args[] = {(void*)&Bd, (void*)&map, (void*)&res, (void*)&ninv, (void*)&batch, (void*)&err, (void*)&spin,
+                        (void*)&extra};
+        return launch(intt_tma_kernel(), "ntt_inv", B.h.logn, grid, dim3(64), intt_tma_smem(), st, args);
+    }
     if (ks.ntt_jobs_per_block == 1) {  // k_ntt1: grid (jobs, primes)
         void* args[] = {(void*)&Bd, (void*)&res, (void*)&ninv, (void*)&batch};
         return launch(ks.ntt[inverse ? 1 : 0], inverse ? "ntt_inv" : "ntt_fwd", B.h.logn, dim3(batch, B.h.k),
@@ -608,6 +619,16 @@ cy_status cy_polymul_batched_status(cy_stream_t stream) { return mixed_status((c
 cy_status cy_ntt(cy_ring* r, uint32_t* d_res, int batch, int inverse, cy_stream_t stream) {
     CY_TRY(validate_poly_args(r, d_res, d_res, d_res, batch));
     return run_ntt(r->plain, d_res, batch, inverse != 0, (cudaStream_t)stream);
+}
+
+cy_status cy_ntt_check(void) {
+    CY_CUDA(cudaDeviceSynchronize());
+    return ntt_tma_check(true);
+}
+
+cy_status cy_ntt_test_wait(unsigned spin_limit, unsigned extra_bytes) {
+    ntt_tma_set_test(spin_limit, extra_bytes);
+    return CY_OK;
 }
 
 cy_status cy_crt(cy_ring* r, const uint64_t* d_x, uint32_t* d_res, int batch, cy_stream_t stream) {

@@ -17,6 +17,7 @@ struct KernelSet {
     size_t smem_mul = 0, smem_ks[2] = {0, 0}, smem_ntt = 0;
     int blocks_per_prime = 1;  // product / keyswitch blocks per (prime, job): 2 for block pairs
     int ntt_jobs_per_block = 2;  // k_ntt: two jobs per block, grid (primes, jobs/2); k_ntt1: one, grid (jobs, primes)
+    bool intt_tma = false;  // N = 4096: the standalone inverse NTT takes its input tile by TMA (k_intt_tma)
     void* mul_for(int l64, bool centered) const { return mul[mul[l64][0] ? l64 : 0][centered ? 1 : 0]; }
     void* ks_for(int l64, int nd4) const { return ks[ks[l64][0] ? l64 : 0][nd4]; }
 };

@@ -1,6 +1,7 @@
 // host.h -- internal host-side objects behind the C ABI.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -106,6 +107,22 @@ int chunk_jobs(int n, int k);
 using ChunkOp = std::function<cy_status(cy_workspace*, const uint64_t*, const uint64_t*, uint64_t*, int, cudaStream_t)>;
 cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* h_in0, const uint64_t* h_in1,
                             uint64_t* h_out, const ChunkOp& op);
+
+// ---- inverse NTT of length 4096 with its input tile by TMA (k_ntt_tma.cu) ----
+void* intt_tma_kernel();
+size_t intt_tma_smem();
+// whether `res` ([jobs][k][4096] words, rows = jobs * k * 64) can be tiled
+bool ntt_tma_usable(const void* res, long long rows);
+// the tensor map of `res`, the grid and the error word of the launch
+cy_status intt_tma_prepare(uint32_t* res, long long rows, int k, int njobs, CUtensorMap* map, dim3* grid,
+                           int** d_err);
+// CY_ERR_TIMEOUT if a launch gave up waiting for a tile since the last check
+cy_status ntt_tma_check(bool reset);
+// polls of the tile wait (default 2^22) and bytes the tile's barrier is told to
+// expect beyond the tile (0; > 0 makes the wait run out, for its test)
+uint32_t ntt_tma_spin_limit();
+uint32_t ntt_tma_extra_tx();
+void ntt_tma_set_test(uint32_t spin_limit, uint32_t extra_tx);
 
 }  // namespace cy
 

@@ -30,6 +30,7 @@ void fill_n14_e4d1(KernelSet& ks);
 void fill_n12_e4u(KernelSet& ks);
 void fill_n14_pair(KernelSet& ks);
 void fill_n12_e6(KernelSet& ks);
+void fill_n12_e6t(KernelSet& ks);
 
 struct VariantTable {
     std::vector<KernelSet> v[LOGN_MAX + 1];
@@ -70,6 +71,7 @@ static const VariantTable& variants() {
         add(14, fill_n14_e4d1);
         add(12, fill_n12_e4u);
         add(12, fill_n12_e6);  // 64 coefficients per thread: two passes, one transpose
+        add(12, fill_n12_e6t);  // the same, the standalone inverse NTT's input by TMA
         {
             KernelSet ks = T.v[14][0];  // the default set's standalone NTT
             fill_n14_pair(ks);

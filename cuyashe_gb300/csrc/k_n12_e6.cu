@@ -7,4 +7,10 @@
 
 namespace cy {
 void fill_n12_e6(KernelSet& ks) { fill_kernel_set<12, 6, true, 6, 6, true, true, 1, 1, 0x4u>(ks); }
+// the same kernels, with the standalone inverse NTT taking its input tile by
+// TMA (k_ntt_tma.cu)
+void fill_n12_e6t(KernelSet& ks) {
+    fill_n12_e6(ks);
+    ks.intt_tma = true;
+}
 }  // namespace cy

@@ -189,8 +189,9 @@ static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, i
                    &chosen);
 }
 
-// The standalone forward transform (cy_ntt) of `batch` residue vectors; each
-// run transforms a fresh copy of the same input so that outputs can be compared.
+// The standalone transforms (cy_ntt) of `batch` residue vectors, inverse then
+// forward (schedules may differ in either direction); each run transforms a
+// fresh copy of the same input and must give it back.
 static cy_status tune_ntt(const Basis& B, int batch, cudaStream_t st) {
     const size_t words = (size_t)batch * B.h.k * B.h.n;
     std::vector<uint32_t> h(words);
@@ -208,6 +209,7 @@ static cy_status tune_ntt(const Basis& B, int batch, cudaStream_t st) {
                        cudaError_t e = cudaMemcpyAsync(out, src.p, words * sizeof(uint32_t),
                                                        cudaMemcpyDeviceToDevice, st);
                        if (e != cudaSuccess) return cuda_error(e, "autotune copy");
+                       CY_TRY(run_ntt_api(B, (uint32_t*)out, batch, true, st, v));
                        return run_ntt_api(B, (uint32_t*)out, batch, false, st, v);
                    },
                    &chosen);

@@ -217,6 +217,19 @@ cy_status cy_mixed_plan_test_starve(cy_mixed_plan *plan, int job, unsigned spin_
  * (src/cuda_functions.cu:447-458). */
 cy_status cy_ntt(cy_ring *ring, uint32_t *d_res, int batch, int inverse, cy_stream_t stream);
 
+/* Status of the standalone NTT's bounded waits: the N = 4096 schedule whose
+ * inverse takes its input tile by TMA waits for each tile on a barrier with a
+ * poll limit, and a block that gives up records CY_ERR_TIMEOUT on the device. This synchronises
+ * the device, returns CY_ERR_TIMEOUT if any launch since the last call gave up
+ * (with cy_last_error saying so) and clears the record. No counterpart in the
+ * reference (it has no failure handling). */
+cy_status cy_ntt_check(void);
+
+/* Testing hook for that path: the next TMA inverse transforms poll at most
+ * spin_limit times (0: the default) and tell the tile's barrier to expect
+ * extra_bytes beyond the tile (0: none; > 0 makes every wait run out). */
+cy_status cy_ntt_test_wait(unsigned spin_limit, unsigned extra_bytes);
+
 /* CRT split and ICRT recombination on their own (callCRT / callICRT,
  * src/cuda_bn.cu:970-1045): d_res [batch][k][N] uint32 <-> d_x [batch][N][L]. */
 cy_status cy_crt(cy_ring *ring, const uint64_t *d_x, uint32_t *d_res, int batch, cy_stream_t stream);
