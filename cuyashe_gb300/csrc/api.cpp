@@ -94,18 +94,21 @@ static std::atomic<int> g_epi_generic{0};
 // ICRT epilogue of basis B over `nj` jobs of residues [job][k][N] into `out`: the
 // kernel specialised for B's prime count (constants passed by value) when there
 // is one, else the generic kernel.
+// lm: outputs limb-major ([job][limb][N]), for the keyswitch that follows in an
+// HE multiply (its digit loads then cover consecutive words)
 static cy_status launch_epi(const Basis& B, const uint32_t* resid, void* out, int nj, cudaStream_t st,
-                            const char* name) {
+                            const char* name, int lm = 0) {
     const BasisDev* Bd = B.d;
     unsigned long long fl = epi_frac_limit();
     const long long coefs = (long long)nj * B.h.n;
     if (B.epi && !g_epi_generic.load()) {
         const long long per = (long long)kEpiThreads * B.epi->coefs_per_thread;
-        void* args[] = {(void*)B.epi_param.data(), (void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
+        void* args[] = {(void*)B.epi_param.data(), (void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl,
+                        (void*)&lm};
         return launch(B.epi->func, name, B.h.logn, dim3((unsigned)((coefs + per - 1) / per)), dim3(kEpiThreads), 0,
                       st, args);
     }
-    void* args[] = {(void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl};
+    void* args[] = {(void*)&Bd, (void*)&resid, (void*)&out, (void*)&nj, (void*)&fl, (void*)&lm};
     return launch(epi_kernel(B.h.l32, B.h.mode), name, B.h.logn, dim3(epi_blocks(coefs, B.h.l32)), dim3(kEpiThreads),
                   0, st, args);
 }
@@ -176,24 +179,27 @@ struct Lanes {
     }
 };
 
-// One chunk of products with basis B: out_j = epilogue(a_j * b_j), residues in `resid`.
+// One chunk of products with basis B: out_j = epilogue(a_j * b_j), residues in
+// `resid`; lm: outputs limb-major.
 static cy_status product_chunk(const Basis& B, const KernelSet& ks, bool centered, const uint64_t* aj,
                                long long a_stride, const uint64_t* bj, long long b_stride, void* oj, int nj,
-                               uint32_t* resid, cudaStream_t st) {
+                               uint32_t* resid, cudaStream_t st, int lm = 0) {
     const int k = B.h.k;
     const BasisDev* Bd = B.d;
     void* args[] = {(void*)&Bd, (void*)&aj, (void*)&a_stride, (void*)&bj, (void*)&b_stride, (void*)&resid};
     CY_TRY(launch(ks.mul_for(B.h.l64, centered), centered ? "mul_centered" : "mul", B.h.logn,
                   dim3(k * ks.blocks_per_prime, nj), dim3(ks.threads), ks.smem_mul, st, args));
-    return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
+    return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode), lm);
 }
 
-// One chunk of keyswitches c_j -> out_j (out may alias c), residues in `resid`.
+// One chunk of keyswitches c_j -> out_j (out may alias c), residues in `resid`;
+// lm: c is limb-major ([job][limb][N]).
 static cy_status keyswitch_chunk(const Basis& B, const KernelSet& ks, int sel, const uint64_t* cj, const uint2* evk,
-                                 int ell, uint64_t* oj, int nj, uint32_t* resid, cudaStream_t st) {
+                                 int ell, uint64_t* oj, int nj, uint32_t* resid, cudaStream_t st, int lm = 0) {
     const int k = B.h.k;
     const BasisDev* Bd = B.d;
-    void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid};
+    int cs = lm ? 1 : B.h.l64, ls = lm ? B.h.n : 1;  // limb w of coefficient i at [i * cs + w * ls]
+    void* args[] = {(void*)&Bd, (void*)&cj, (void*)&evk, (void*)&ell, (void*)&resid, (void*)&cs, (void*)&ls};
     CY_TRY(launch(ks.ks_for(B.h.l64, sel), "keyswitch", B.h.logn, dim3(k * ks.blocks_per_prime, nj),
                   dim3(ks.threads), ks.smem_ks[sel], st, args));
     return launch_epi(B, resid, oj, nj, st, epi_name(B.h.mode));
@@ -233,8 +239,10 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
 // keyswitch of `batch` polynomials c_j -> out_j (may alias c)
 // chunk_k > 0 sizes the chunks as for a basis of that many primes (the tuner
 // uses the HE multiply's chunks, which are sized by its larger basis).
+// lm: c is limb-major (the tuner times the layout of the HE multiply's keyswitch)
 static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out,
-                               int batch, Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0) {
+                               int batch, Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0,
+                               int lm = 0) {
     if (batch == 0) return CY_OK;
     const KernelSet& ks =
         kernel_variant(B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, TUNE_KS));
@@ -249,7 +257,7 @@ static cy_status run_keyswitch(const Basis& B, const uint64_t* c, const uint2* e
     for (int cc = 0; cc < nchunks && status == CY_OK; cc++) {
         const int j0 = cc * chunk, nj = std::min(chunk, batch - j0);
         status = keyswitch_chunk(B, ks, sel, c + (size_t)j0 * n * l64, evk, ell, out + (size_t)j0 * n * l64, nj,
-                                 L.scratch(cc), L.stream(cc));
+                                 L.scratch(cc), L.stream(cc), lm);
     }
     return L.end(ws, st, status);
 }
@@ -275,10 +283,13 @@ cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* ev
     for (int c = 0; c < nchunks && status == CY_OK; c++) {
         const int j0 = c * chunk, nj = std::min(chunk, batch - j0);
         uint64_t* oj = out + (size_t)j0 * stride;
+        // with relinearisation the rounded tensor product goes to `out` limb-major
+        // (coalesced digit loads in the keyswitch), and the keyswitch's epilogue
+        // writes the result over it in the [N][limb] layout
         status = product_chunk(tensor, kt, true, c1 + (size_t)j0 * stride, stride, c2 + (size_t)j0 * stride, stride,
-                               oj, nj, L.scratch(c), L.stream(c));
+                               oj, nj, L.scratch(c), L.stream(c), do_relin ? 1 : 0);
         if (status == CY_OK && do_relin)
-            status = keyswitch_chunk(relin, kr, sel, oj, evk, ell, oj, nj, L.scratch(c), L.stream(c));
+            status = keyswitch_chunk(relin, kr, sel, oj, evk, ell, oj, nj, L.scratch(c), L.stream(c), 1);
     }
     return L.end(ws, st, status);
 }
@@ -367,8 +378,8 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
 }
 
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st, int variant, int chunk_k) {
-    return run_keyswitch(B, c, evk, ell, out, batch, ws, st, variant, chunk_k);
+                            Workspace& ws, cudaStream_t st, int variant, int chunk_k, int lm) {
+    return run_keyswitch(B, c, evk, ell, out, batch, ws, st, variant, chunk_k, lm);
 }
 
 // Evaluation key in the keyswitch basis, NTT domain, with Shoup companions:

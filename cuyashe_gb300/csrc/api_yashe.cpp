@@ -24,7 +24,7 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
 cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* evk, int ell, const uint64_t* c1,
                         const uint64_t* c2, uint64_t* out, int batch, bool do_relin, Workspace& ws, cudaStream_t st);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0);
+                            Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0, int lm = 0);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 cy_status host_keygen(cy_yashe* y, uint64_t seed, std::vector<uint64_t>& f, std::vector<uint64_t>& h,
                       std::vector<uint64_t>& evk);

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : mul
 template <int LOGN, int LOGE, int L64, int ND, int MINB = 0, bool SINGLE = false>
 __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_min_blocks<LOGN, LOGE>()))
     k_keyswitch(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
-                int ell, uint32_t* __restrict__ resid) {
+                int ell, uint32_t* __restrict__ resid, int cs, int ls) {
     using PL = NttPlan<LOGN, LOGE>;
     constexpr int E = PL::E;
     constexpr int LAST = PL::NPASS - 1;
@@ -290,6 +290,10 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
     const uint64_t* cj = C + (size_t)job * PL::N * l64;
+    // limb w of coefficient pos at cj[pos * cs + w * ls]: (cs, ls) = (limbs, 1) for
+    // [N][limb], (1, N) for limb-major (the HE multiply's intermediate: a warp's
+    // loads of one limb are then contiguous). Kernel parameters, so that they stay
+    // in the constant bank.
     constexpr int STRIDE = SINGLE ? 0 : region_stride<PL, ND>();
 
     uint32_t acc[1][E];
@@ -304,18 +308,23 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
             if constexpr (L64 > 0 && ND % 2 == 0) {
                 // digits d0 .. d0+ND-1 are limbs d0/2 .. d0/2+ND/2-1 of the coefficient;
                 // digits past the last word of q are zero (coefficients are < q)
-                const uint64_t* src = cj + (size_t)pos * L64 + (d0 >> 1);
+                const uint64_t* src = cj + (size_t)pos * cs + (size_t)(d0 >> 1) * ls;
                 uint32_t w[ND];
+                bool both = false;  // two limbs side by side: one 16-byte load
                 if constexpr (ND == 4 && L64 % 2 == 0) {
-                    const uint4 v = __ldg(reinterpret_cast<const uint4*>(src));
-                    w[0] = v.x;
-                    w[1] = v.y;
-                    w[2] = v.z;
-                    w[3] = v.w;
-                } else {
+                    if (ls == 1) {
+                        const uint4 v = __ldg(reinterpret_cast<const uint4*>(src));
+                        w[0] = v.x;
+                        w[1] = v.y;
+                        w[ND - 2] = v.z;
+                        w[ND - 1] = v.w;
+                        both = true;
+                    }
+                }
+                if (!both) {
 #pragma unroll
                     for (int o = 0; o < ND; o += 2) {
-                        const uint2 v = __ldg(reinterpret_cast<const uint2*>(src) + (o >> 1));
+                        const uint2 v = __ldg(reinterpret_cast<const uint2*>(src + (o >> 1) * ls));
                         w[o] = v.x;
                         w[o + 1] = v.y;
                     }
@@ -328,7 +337,7 @@ __global__ void __launch_bounds__(NttPlan<LOGN, LOGE>::G, (MINB > 0 ? MINB : ks_
                     const int d = d0 + o;
                     uint32_t w = 0;
                     if (d < ell) {
-                        const uint64_t limb = __ldg(cj + (size_t)pos * l64 + (d >> 1));
+                        const uint64_t limb = __ldg(cj + (size_t)pos * cs + (size_t)(d >> 1) * ls);
                         w = (uint32_t)(limb >> (32 * (d & 1)));
                     }
                     x[o][e] = red(w, 2 * p);  // digit < 2^32 < 6p -> [0, 4p)
@@ -770,10 +779,12 @@ __device__ __noinline__ uint64_t yashe_round_exact(const EpiShared& S, const Bas
 // unless the fraction of Z is within 2^-28 of the next integer; those
 // coefficients (about one in 2^28), and all of them when frac_limit is 0, take
 // the exact multiword path.
+// lstride: distance in words between the limbs of an output coefficient (1, or
+// N for the limb-major layout)
 template <int L, int MODE, int C>
 __device__ __forceinline__ void epi_coefs(const EpiShared& S, const BasisDev* __restrict__ B,
                                           const uint32_t* const (&r0)[C], size_t stride, uint64_t* const (&dst)[C],
-                                          const bool (&store)[C], uint64_t frac_limit) {
+                                          const bool (&store)[C], uint64_t frac_limit, size_t lstride = 1) {
     const int k = B->k, shift = B->shift, l64 = B->l64;
     const int groups = (k + 2) / 3;
     const uint64_t mu = B->mu;
@@ -879,7 +890,7 @@ __device__ __forceinline__ void epi_coefs(const EpiShared& S, const BasisDev* __
             for (int j = 0; j < (L + 1) / 2; j++) {
                 const uint64_t lo32 = o[2 * j];
                 const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
-                if (j < l64) dst[c][j] = lo32 | (hi32 << 32);
+                if (j < l64) dst[c][j * lstride] = lo32 | (hi32 << 32);
             }
         }
     }
@@ -896,9 +907,12 @@ __device__ __forceinline__ void epi_coef(const EpiShared& S, const BasisDev* __r
     epi_coefs<L, MODE, 1>(S, B, rr, stride, dd, st, frac_limit);
 }
 
+// lm: outputs limb-major ([job][limb][N]) instead of [job][N][limb] (modes
+// MODQ and YASHE; the HE multiply's intermediate before its keyswitch)
 template <int L, int MODE>
 __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
-                                             void* __restrict__ out, int njobs, unsigned long long frac_limit) {
+                                             void* __restrict__ out, int njobs, unsigned long long frac_limit,
+                                             int lm) {
     constexpr int C = epi_coefs_per_thread(L);  // coefficients per thread
     __shared__ EpiShared S;
     epi_stage<L, MODE>(S, B, threadIdx.x, blockDim.x);
@@ -920,9 +934,10 @@ __global__ void __launch_bounds__(256) k_epi(const BasisDev* __restrict__ B, con
         const int coef = (int)(idx & (n - 1));
         r0[c] = resid + (size_t)job * k * n + coef;
         dst[c] = reinterpret_cast<uint64_t*>(out) +
-                 (MODE == EPI_DECRYPT ? (size_t)job * n + coef : ((size_t)job * n + coef) * l64);
+                 (MODE == EPI_DECRYPT ? (size_t)job * n + coef
+                                      : (size_t)job * n * l64 + (lm ? (size_t)coef : (size_t)coef * l64));
     }
-    epi_coefs<L, MODE, C>(S, B, r0, (size_t)n, dst, store, frac_limit);
+    epi_coefs<L, MODE, C>(S, B, r0, (size_t)n, dst, store, frac_limit, lm ? (size_t)n : 1);
 }
 
 // --------------------------------------------------------------------------
@@ -971,7 +986,8 @@ __device__ __noinline__ uint64_t yashe_round_exact_g(const BasisDev* __restrict_
 template <int L, int MODE, int K, int C>
 __global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<L, K> P,
                                                const BasisDev* __restrict__ B, const uint32_t* __restrict__ resid,
-                                               void* __restrict__ out, int njobs, unsigned long long frac_limit) {
+                                               void* __restrict__ out, int njobs, unsigned long long frac_limit,
+                                               int lm) {
     static_assert(MODE == EPI_MODQ || MODE == EPI_YASHE, "mod-q and YASHE epilogues only");
     const int logn = P.logn;
     const int n = 1 << logn;
@@ -989,8 +1005,10 @@ __global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<
         const long long job = idx >> logn;
         const int coef = (int)(idx & (n - 1));
         r0[c] = resid + (size_t)job * K * n + coef;
-        dst[c] = reinterpret_cast<uint64_t*>(out) + ((size_t)job * n + coef) * P.l64;
+        dst[c] = reinterpret_cast<uint64_t*>(out) + (size_t)job * n * P.l64 +
+                 (lm ? (size_t)coef : (size_t)coef * P.l64);
     }
+    const size_t lstride = lm ? (size_t)n : 1;
     uint32_t r[K][C];
 #pragma unroll
     for (int i = 0; i < K; i++)
@@ -1067,7 +1085,7 @@ __global__ void __launch_bounds__(256) k_epi_k(const __grid_constant__ EpiConst<
         for (int j = 0; j < (L + 1) / 2; j++) {
             const uint64_t lo32 = o[2 * j];
             const uint64_t hi32 = (2 * j + 1 < L) ? o[2 * j + 1] : 0u;
-            if (j < P.l64) dst[c][j] = lo32 | (hi32 << 32);
+            if (j < P.l64) dst[c][j * lstride] = lo32 | (hi32 << 32);
         }
     }
 }

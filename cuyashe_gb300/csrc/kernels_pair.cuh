@@ -149,7 +149,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
 template <int L64, int ND>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
     k_keyswitch_pair(const BasisDev* __restrict__ B, const uint64_t* __restrict__ C, const uint2* __restrict__ evk,
-                     int ell, uint32_t* __restrict__ resid) {
+                     int ell, uint32_t* __restrict__ resid, int cs, int ls) {
     using PL = PairPlan;
     constexpr int E = PL::E;
     constexpr int LAST = PL::NPASS - 1;
@@ -165,6 +165,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
     const uint2* __restrict__ psi = B->psi[prime];
     const uint2* __restrict__ ipsi = B->ipsi[prime];
     const uint64_t* cj = C + (size_t)job * (2 * kPairHalf) * l64;
+    // limb w of coefficient pos at cj[pos * cs + w * ls]: (limbs, 1) for [N][limb],
+    // (1, N) for limb-major
     uint32_t* recv = smem + region_bytes<PL, ND>() / 4;
     constexpr int STRIDE = region_stride<PL, ND>();
     const int tm = 2 + (int)h;
@@ -186,8 +188,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairPlan::G, 1)
                 const int d = d0 + o;
                 uint32_t wl = 0, wh = 0;
                 if (L64 > 0 || d < ell) {  // digits past the top word of q are zero
-                    const uint64_t ll = __ldg(cj + (size_t)pos * l64 + (d >> 1));
-                    const uint64_t lh = __ldg(cj + (size_t)(pos + kPairHalf) * l64 + (d >> 1));
+                    const uint64_t ll = __ldg(cj + (size_t)pos * cs + (size_t)(d >> 1) * ls);
+                    const uint64_t lh = __ldg(cj + (size_t)(pos + kPairHalf) * cs + (size_t)(d >> 1) * ls);
                     wl = (uint32_t)(ll >> (32 * (d & 1)));
                     wh = (uint32_t)(lh >> (32 * (d & 1)));
                 }

@@ -100,7 +100,8 @@ extern "C" cy_status cy_polymul_noalloc(cy_ring* r, const uint64_t* d_a, const u
                           dim3(ks.threads), ks.smem_mul, st, args));
     void* epi = epi_kernel(B.h.l32, EPI_MODQ);
     unsigned long long fl = 0;  // mod-q epilogue: no rounding estimate
-    void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch, (void*)&fl};
+    int lm = 0;                 // outputs in the [job][N][limb] layout
+    void* eargs[] = {(void*)&Bd, (void*)&scratch, (void*)&d_c, (void*)&batch, (void*)&fl, (void*)&lm};
     const long long threads = (long long)batch * n;
     const long long per = 256ll * epi_coefs_per_thread(B.h.l32);
     return launch_noalloc(epi, "epi_modq_noalloc", B.h.logn, dim3((unsigned)((threads + per - 1) / per)), dim3(256),

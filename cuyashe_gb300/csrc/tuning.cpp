@@ -30,7 +30,7 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
                           cudaStream_t st, int variant);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
-                            Workspace& ws, cudaStream_t st, int variant, int chunk_k);
+                            Workspace& ws, cudaStream_t st, int variant, int chunk_k, int lm);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 
 cy_status run_ntt_api(const Basis& B, uint32_t* res, int batch, bool inverse, cudaStream_t st, int variant);
@@ -183,8 +183,9 @@ static cy_status tune_keyswitch(const Basis& relin, const uint2* evk, int ell, i
     int chosen = 0;
     return tune_op(relin.h.logn, l64, TUNE_KS, bytes, st,
                    [&](int v, void* out) {
+                       // the HE multiply's layout: its intermediate is limb-major
                        return run_keyswitch_api(relin, (const uint64_t*)c.p, evk, ell, (uint64_t*)out, batch, ws, st,
-                                                v, chunk_k);
+                                                v, chunk_k, 1);
                    },
                    &chosen);
 }
