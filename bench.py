@@ -1011,6 +1011,9 @@ def ncu_schedules(batch: int = 1024, only: str = "all"):
     """One call of every N = 4096 schedule of the product (plain and centred),
     the keyswitch and the standalone NTT (forced with cy_tuning_import) between
     cudaProfilerStart/Stop, for ncu's per-schedule counts; prints the order.
+    `ksm=v` runs keyswitch schedule v inside an HE multiply of one chunk (170
+    pairs: the tensor residues of 24 MiB), where its input is limb-major; a
+    capture filtered to k_keyswitch then has one launch per such schedule.
     `only`: "all", or a comma-separated list such as "mulc=7,ks=5,ntt=9"."""
     import numpy as np
     import torch
@@ -1039,18 +1042,22 @@ def ncu_schedules(batch: int = 1024, only: str = "all"):
     O = Y.ring.empty(batch)
     RES = torch.zeros((batch, R.k, N), dtype=torch.int32, device="cuda")
     plan = [(op, v) for op in ("mul", "mulc", "ks", "ntt") for v in variants(op)]
+    plan += [("ksm", v) for v in variants("ks")]
+    KSM = 170
     if only != "all":
         want = {tuple(x.split("=")) for x in only.split(",")}
         plan = [(op, v) for op, v in plan if (op, str(v)) in want]
 
     def run(op, v):
-        cy.tuning_import("n%d.l2.%s=%d" % (N, op, v))
+        cy.tuning_import("n%d.l2.%s=%d" % (N, "ks" if op == "ksm" else op, v))
         if op == "mul":
             R.polymul(A, Bt, out=O)
         elif op == "mulc":
             Y.mul(A, Bt, relin=False, out=O)
         elif op == "ks":
             Y.keyswitch(A, out=O)
+        elif op == "ksm":
+            Y.mul(A[:KSM], Bt[:KSM], relin=True, out=O[:KSM])
         else:
             R.ntt(RES)
             R.ntt(RES, inverse=True)
