@@ -92,6 +92,11 @@ def test_every_tensor_and_keyswitch_schedule_matches_oracle(cy):
         out = R.download(Y.keyswitch(R.upload([exp_t])))
         torch.cuda.synchronize()
         assert list(out[0]) == exp_r, "keyswitch schedule %d" % v
+        # inside the HE multiply the keyswitch reads the tensor product limb-major
+        out = R.download(Y.mul(C1, C2, relin=True))
+        torch.cuda.synchronize()
+        assert list(out[0]) == exp_r, "keyswitch schedule %d inside the HE multiply" % v
+    cy.tuning_import("n%d.l%d.mulc=0;n%d.l%d.ks=0" % (n, R.L, n, R.L))
 
 
 def test_every_keyswitch_schedule_at_16384_matches_oracle(cy):
