@@ -594,7 +594,7 @@ def run_ours(args):
     Y = cy.Yashe(N, Q_YASHE, T, W_BITS, 8.0)
     Y.keygen(1234 + rank)
     if not args.no_autotune:
-        Y.autotune(batch=512)
+        Y.autotune(batch=B)  # the schedules that are fastest at the step's own batch
     tuning = cy.tuning_export()
     # weak scaling: each rank multiplies its own contiguous share (B pairs) of the
     # job's world * B pairs; no data-path collective

@@ -22,9 +22,11 @@ cy_status run_product_api(const Basis& B, bool centered, const uint64_t* a, long
                           long long b_stride, void* out, long long out_stride, int batch, Workspace& ws,
                           cudaStream_t st, int variant = -1);
 cy_status run_yashe_mul(const Basis& tensor, const Basis& relin, const uint2* evk, int ell, const uint64_t* c1,
-                        const uint64_t* c2, uint64_t* out, int batch, bool do_relin, Workspace& ws, cudaStream_t st);
+                        const uint64_t* c2, uint64_t* out, int batch, bool do_relin, Workspace& ws, cudaStream_t st,
+                        int ks_variant = -1);
 cy_status run_keyswitch_api(const Basis& B, const uint64_t* c, const uint2* evk, int ell, uint64_t* out, int batch,
                             Workspace& ws, cudaStream_t st, int variant = -1, int chunk_k = 0, int lm = 0);
+int yashe_chunk_jobs(const Basis& tensor, const Basis& relin, int ell, bool do_relin);
 cy_status prepare_evk(const Basis& relin, const uint64_t* h_evk, int ell, int n, int l64, uint2** d_evk);
 cy_status host_keygen(cy_yashe* y, uint64_t seed, std::vector<uint64_t>& f, std::vector<uint64_t>& h,
                       std::vector<uint64_t>& evk);
@@ -203,7 +205,8 @@ cy_status cy_yashe_mul_host(cy_yashe* y, const uint64_t* h_c1, const uint64_t* h
     if (relin && !y->has_keys) return set_error(CY_ERR_NO_KEYS, "relinearisation needs keys");
     if (batch == 0) return CY_OK;
     cy_ring* r = y->ring;
-    return run_host_pipeline((size_t)r->n * r->l64, batch, chunk_jobs(r->n, y->tensor.h.k), h_c1, h_c2, h_out,
+    return run_host_pipeline((size_t)r->n * r->l64, batch, yashe_chunk_jobs(y->tensor, y->relin, y->ell, relin != 0),
+                             h_c1, h_c2, h_out,
                              [y, relin](cy_workspace* ws, const uint64_t* a, const uint64_t* b, uint64_t* c, int nj,
                                         cudaStream_t st) { return cy_yashe_mul_ws(y, ws, a, b, c, nj, relin, st); });
 }

@@ -108,6 +108,10 @@ using ChunkOp = std::function<cy_status(cy_workspace*, const uint64_t*, const ui
 cy_status run_host_pipeline(size_t words, int batch, int chunk, const uint64_t* h_in0, const uint64_t* h_in1,
                             uint64_t* h_out, const ChunkOp& op);
 
+// *differ: whether the bytes at a and b (multiple of 4) differ; synchronises `st`;
+// d_flag: one device int of scratch (k_misc.cu)
+cy_status words_differ(const void* a, const void* b, size_t bytes, int* d_flag, cudaStream_t st, bool* differ);
+
 // ---- inverse NTT of length 4096 with its input tile by TMA (k_ntt_tma.cu) ----
 void* intt_tma_kernel();
 size_t intt_tma_smem();

@@ -2,6 +2,8 @@
 #include <mutex>
 #include <vector>
 
+#include <algorithm>
+
 #include "host.h"
 #include "kernels.cuh"
 
@@ -235,6 +237,29 @@ __global__ void k_poly_move(uint64_t* const* __restrict__ ptrs, uint64_t* __rest
 
 int trace_begin(const char* name, int logn, cudaStream_t st);
 void trace_end(int idx, cudaStream_t st);
+
+// Sets *differ to 1 if the `words` 32-bit words at a and b are not all equal
+// (the autotuner's check that a schedule gives the default's output).
+__global__ void k_words_differ(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t words,
+                               int* __restrict__ differ) {
+    bool d = false;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        d |= a[i] != b[i];
+    if (__syncthreads_or(d) && threadIdx.x == 0) atomicExch(differ, 1);
+}
+
+cy_status words_differ(const void* a, const void* b, size_t bytes, int* d_flag, cudaStream_t st, bool* differ) {
+    size_t words = bytes / 4;
+    CY_CUDA(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
+    const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((words + 255) / 256, 4096));
+    void* args[] = {(void*)&a, (void*)&b, (void*)&words, (void*)&d_flag};
+    CY_CUDA(cudaLaunchKernel((void*)k_words_differ, dim3(blocks), dim3(256), args, 0, st));
+    int h = 0;
+    CY_CUDA(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CY_CUDA(cudaStreamSynchronize(st));
+    *differ = h != 0;
+    return CY_OK;
+}
 
 cy_status move_polys(uint64_t* const* d_ptrs, uint64_t* flat, int count, size_t words, bool gather,
                      cudaStream_t st) {
