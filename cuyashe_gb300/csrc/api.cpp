@@ -92,14 +92,22 @@ static int resident_blocks(void* func, int threads, size_t smem) {
     return cache[std::make_tuple(func, dev, threads)] = per_sm * sms;
 }
 
-// A chunk of `jobs` rounded down to whole waves of a kernel that runs `per_job`
-// blocks per job, so that its last wave is not a tail (unchanged when it holds
-// less than one wave). At N = 4096 with the 64-coefficient keyswitch: 912 slots,
-// 6 blocks per job, chunks of 152 jobs instead of 170 (2.91 against 2.97 ms per
-// 4096-pair HE multiply step).
+// A chunk of `jobs` cut to whole waves of a kernel that runs `per_job` blocks per
+// job, so that its last wave is not a tail: up to the next whole wave when that is
+// at most a quarter more (the size target is soft), else down (unchanged when it
+// holds less than one wave). At N = 4096 with the 64-coefficient keyswitch: 912
+// slots, 6 blocks per job, chunks of 152 jobs instead of 170 (2.91 against 2.97 ms
+// per 4096-pair HE multiply step). CY_WAVE_CHUNKS=0 turns this off.
 static int wave_chunk(int jobs, void* func, int threads, size_t smem, int per_job) {
-    const int w = per_job > 0 ? resident_blocks(func, threads, smem) / per_job : 0;
-    return (w >= 1 && jobs > w) ? jobs / w * w : jobs;
+    static const bool on = [] {
+        const char* e = std::getenv("CY_WAVE_CHUNKS");
+        return !(e && std::atoi(e) == 0);
+    }();
+    const int w = (on && per_job > 0) ? resident_blocks(func, threads, smem) / per_job : 0;
+    if (w < 1 || jobs <= w) return jobs;
+    const long long up = ((long long)jobs + w - 1) / w * w;
+    if (4 * up <= 5ll * jobs && up <= 65535) return (int)up;
+    return jobs / w * w;
 }
 
 static cy_status launch(void* func, const char* name, int logn, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
