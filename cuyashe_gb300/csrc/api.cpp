@@ -255,6 +255,11 @@ static cy_status keyswitch_digits_per_pass(const KernelSet& ks, int ell, int* se
     return CY_OK;
 }
 
+// a product chunk cut to whole waves of the product kernel
+static int product_chunk_jobs(const Basis& B, const KernelSet& ks, bool centered, int jobs) {
+    return wave_chunk(jobs, ks.mul_for(B.h.l64, centered), ks.threads, ks.smem_mul, B.h.k * ks.blocks_per_prime);
+}
+
 // products of `batch` jobs with basis B: out_j = epilogue(a_j * b_j); `variant`
 // selects the NTT schedule (-1: the tuned one for this device and size)
 static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, long long a_stride,
@@ -264,7 +269,7 @@ static cy_status run_product(const Basis& B, bool centered, const uint64_t* a, l
     const KernelSet& ks = kernel_variant(
         B.h.logn, variant >= 0 ? variant : tuned_variant(B.h.logn, B.h.l64, centered ? TUNE_MULC : TUNE_MUL));
     const int n = B.h.n, k = B.h.k;
-    const int chunk = std::min(batch, chunk_jobs(n, k));
+    const int chunk = product_chunk_jobs(B, ks, centered, std::min(batch, chunk_jobs(n, k)));
     const int nchunks = (batch + chunk - 1) / chunk;
     Lanes L;
     CY_TRY(L.begin(ws, st, (size_t)chunk * k * n, nchunks));
@@ -599,7 +604,9 @@ cy_status cy_polymul(cy_ring* r, const uint64_t* d_a, const uint64_t* d_b, uint6
 cy_status cy_polymul_host(cy_ring* r, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_c, int batch) {
     CY_TRY(validate_poly_args(r, h_a, h_b, h_c, batch));
     if (batch == 0) return CY_OK;
-    return run_host_pipeline((size_t)r->n * r->l64, batch, chunk_jobs(r->n, r->mul.h.k), h_a, h_b, h_c,
+    const KernelSet& ks = kernel_variant(r->mul.h.logn, tuned_variant(r->mul.h.logn, r->mul.h.l64, TUNE_MUL));
+    const int chunk = product_chunk_jobs(r->mul, ks, false, chunk_jobs(r->n, r->mul.h.k));
+    return run_host_pipeline((size_t)r->n * r->l64, batch, chunk, h_a, h_b, h_c,
                              [r](cy_workspace* ws, const uint64_t* a, const uint64_t* b, uint64_t* c, int nj,
                                  cudaStream_t st) { return cy_polymul_ws(r, ws, a, b, c, nj, st); });
 }
