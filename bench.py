@@ -593,7 +593,9 @@ def run_ours(args):
     # ---- set-up (untimed): keys, schedule autotuning, fresh encryptions --------
     Y = cy.Yashe(N, Q_YASHE, T, W_BITS, 8.0)
     Y.keygen(1234 + rank)
-    if not args.no_autotune:
+    if args.schedules:  # pinned (a profiled run: timings under ncu would mislead the tuner)
+        cy.tuning_import(args.schedules)
+    elif not args.no_autotune:
         Y.autotune(batch=B)  # the schedules that are fastest at the step's own batch
     tuning = cy.tuning_export()
     # weak scaling: each rank multiplies its own contiguous share (B pairs) of the
@@ -1132,6 +1134,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="ciphertext pairs per GPU per step")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT schedules")
+    ap.add_argument("--schedules", default="", metavar="TUNING",
+                    help="schedules to use instead of autotuning (cy_tuning_export format)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-deep", action="store_true", help="skip the N=16384 / 380-bit measurement")
     ap.add_argument("--serving-only", type=float, default=0.0, metavar="SECONDS",
