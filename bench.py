@@ -685,16 +685,19 @@ def run_ours(args):
         Y.mul_host(H1, H2, out=HO, relin=True)
 
     e2e_step()
-    # a longer window than the device timing: host-memory traffic from other
-    # tenants of the machine stalls the copies now and then, and the mean over
-    # ~0.3 s of calls is steadier than over a few
-    e2e_steps = max(3, 2 * args.steps)
+    # four windows of calls, the median window reported: host-memory traffic from
+    # other tenants of the machine stalls the copies now and then, and one stall
+    # should not set the figure (every window's rate is in the line)
+    e2e_per_window = max(3, args.steps // 2)
+    e2e_windows = []
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_ms = (time.perf_counter() - t0) * 1000.0
-    e2e_rate = B * e2e_steps / (e2e_ms / 1000.0)
+    for _ in range(4):
+        t0 = time.perf_counter()
+        for _ in range(e2e_per_window):
+            e2e_step()
+        e2e_windows.append(B * e2e_per_window / (time.perf_counter() - t0))
+    e2e_steps = 4 * e2e_per_window
+    e2e_rate = statistics.median(e2e_windows)
     e2e_ok = torch.equal(HO, OUT.cpu())
     # copy bandwidth on its own (what bounds e2e when the copies outlast the kernels)
     Dtmp = torch.empty_like(C1)
@@ -984,7 +987,9 @@ def run_ours(args):
         "clocks": clk,
         "e2e": {"value": e2e_rate, "unit": "HE mults/s", "h2d_bytes_per_step": 2 * B * CT_BYTES,
                 "d2h_bytes_per_step": B * CT_BYTES, "output_matches_device": e2e_ok,
-                "api": "cy_yashe_mul_host (page-locked host buffers, host wall clock)", "copy_alone": copy_gbs},
+                "api": "cy_yashe_mul_host (page-locked host buffers, host wall clock)", "copy_alone": copy_gbs,
+                "windows_per_s": [round(w) for w in e2e_windows], "calls_per_window": e2e_per_window,
+                "statistic": "median of the windows"},
         "gpu_launches": launches,
         "roofline": roofline,
         "int_roofline": int_roof,
