@@ -696,7 +696,6 @@ def run_ours(args):
         for _ in range(e2e_per_window):
             e2e_step()
         e2e_windows.append(B * e2e_per_window / (time.perf_counter() - t0))
-    e2e_steps = 4 * e2e_per_window
     e2e_rate = statistics.median(e2e_windows)
     e2e_ok = torch.equal(HO, OUT.cpu())
     # copy bandwidth on its own (what bounds e2e when the copies outlast the kernels)
