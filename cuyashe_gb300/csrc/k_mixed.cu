@@ -98,7 +98,7 @@ __device__ __forceinline__ void mixed_ks_unit(const MixedJob& J, const MixedUnit
     uint32_t* sm = smem + sub * SUBW;
     const BasisDev* __restrict__ B = J.B2;
     const Mod m = LOGE == 3 ? mod_of(B->p[prime]) : load_mod(B, prime);
-    const int l64 = J.l64, k2 = J.k2, ell = J.ell;
+    const int k2 = J.k2, ell = J.ell;
     uint32_t acc[1][E];
 #pragma unroll
     for (int e = 0; e < E; e++) acc[0][e] = 0;
@@ -112,9 +112,9 @@ __device__ __forceinline__ void mixed_ks_unit(const MixedJob& J, const MixedUnit
             for (int o = 0; o < 2; o++) {
                 const int d = d0 + o;
                 uint32_t w = 0;
-                if (d < ell) {
+                if (d < ell) {  // c is limb-major here ([limb][N]): a warp's loads are contiguous
                     const uint64_t limb = __ldcg(reinterpret_cast<const unsigned long long*>(J.c) +
-                                                 (size_t)pos * l64 + (d >> 1));
+                                                 (size_t)(d >> 1) * PL::N + pos);
                     w = (uint32_t)(limb >> (32 * (d & 1)));
                 }
                 x[o][e] = __viaddmin_u32(w, m.np2, w);  // digit < 2^32 < 6p -> [0, 4p)
@@ -152,6 +152,9 @@ __device__ __forceinline__ void mixed_epi_coefs(const MixedJob& J, const BasisDe
     epi_stage<L, MODE>(S, B, threadIdx.x, threads);
     __syncthreads();
     const size_t n = (size_t)1 << J.logn;
+    // a job with a keyswitch gets its first epilogue's output limb-major (the
+    // keyswitch units' digit loads), and the keyswitch's epilogue writes over it
+    const bool lm = U.kind == 1 && J.k2 > 0;
     const int end = U.first + U.count;
     for (int c0 = U.first + threadIdx.x; c0 < end; c0 += C * threads) {
         const uint32_t* r0[C];
@@ -163,9 +166,9 @@ __device__ __forceinline__ void mixed_epi_coefs(const MixedJob& J, const BasisDe
             st[c] = coef < end;
             if (!st[c]) coef = c0;  // computed and not written
             r0[c] = J.resid + coef;
-            dst[c] = J.c + (size_t)coef * J.l64;
+            dst[c] = J.c + (lm ? (size_t)coef : (size_t)coef * J.l64);
         }
-        epi_coefs<L, MODE, C>(S, B, r0, n, dst, st, frac_limit);
+        epi_coefs<L, MODE, C>(S, B, r0, n, dst, st, frac_limit, lm ? n : 1);
     }
 }
 
